@@ -1,0 +1,472 @@
+#!/usr/bin/env python
+"""Benchmark of the so3g ProjectionEngine hot path on GB300.
+
+Workload (default "cfg2"): CAR TQU NonTiled map 3 x 2000 x 2000 float64 at
+1 arcmin, 1000 detectors (hexagonal focal plane, radius 1.5 deg) x
+1,000,000 samples at 200 Hz of a constant-elevation scan (el 50 deg, az
+180 +- 10 deg at 1 deg/s), signal float32 N(0,1) plus 1/f noise (knee
+1 Hz).  Seeded synthetic data (numpy default_rng(0) for the focal plane,
+a seeded CUDA generator for the TOD).
+
+One step = to_map + from_map over all samples (the metric's "to_map/from_map
+TOD samples/s").  value = samples per second of the step, inputs resident
+in HBM; e2e = the same through the public API with host (pinned) buffers,
+host<->device copies inside the timed region.  The 4 GB TOD is larger than
+L2, so no L2 flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Under torchrun (N > 1) every rank runs an independent replica of the
+workload on its own GPU (the path needs no exchange); the step time is the
+max over ranks and value counts the samples of all ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    "cfg1": dict(n_det=64, n_time=100_000, radius=1.0, shape=(600, 600), noise=False),
+    "cfg2": dict(n_det=1000, n_time=1_000_000, radius=1.5, shape=(2000, 2000), noise=True),
+}
+METRIC = "to_map/from_map TOD samples/s (CAR TQU) mixed vs FP64 GPU path, % HBM peak"
+ARCMIN = np.pi / 180 / 60
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="cfg2", choices=list(CONFIGS))
+    ap.add_argument("--n-det", type=int, default=None)
+    ap.add_argument("--n-time", type=int, default=None)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64-path", action="store_true")
+    ap.add_argument("--ops", default="to_map,from_map",
+                    help="operations timed in a step (profiling runs pick one)")
+    return ap.parse_args()
+
+
+def config(args):
+    c = dict(CONFIGS[args.config])
+    if args.n_det:
+        c["n_det"] = args.n_det
+    if args.n_time:
+        c["n_time"] = args.n_time
+    return c
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def host_inputs(c, seed=0):
+    """Boresight (native frame), detectors, responses and the geometry."""
+    from so3g_gb300 import synth
+    rng = np.random.default_rng(seed)
+    dets, resp, gamma = synth.focal_plane(rng, c["n_det"], c["radius"])
+    Q, t = synth.scan(c["n_time"], rate=200., el=50., az0=180., throw=10., v_az=1.)
+    p = synth.car_projectionist(c["shape"], ARCMIN, el=50., az0=180.)
+    q = synth.native(p, Q)
+    return p, q, dets, resp
+
+
+def make_signal(torch, c, dev, seed=0):
+    """float32 N(0,1) TOD (+ 1/f noise, knee 1 Hz, alpha -2) on the GPU."""
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    sig = torch.randn((c["n_det"], c["n_time"]), generator=g, device=dev, dtype=torch.float32)
+    if c["noise"]:
+        f = torch.fft.rfftfreq(c["n_time"], d=1 / 200., device=dev)
+        amp = torch.sqrt(1 + (1.0 / torch.clamp(f, min=1e-12)) ** 2)
+        amp[0] = 0.
+        for a in range(0, c["n_det"], 32):
+            b = min(c["n_det"], a + 32)
+            w = torch.randn((b - a, c["n_time"]), generator=g, device=dev, dtype=torch.float32)
+            sig[a:b] += torch.fft.irfft(torch.fft.rfft(w) * amp, n=c["n_time"]).float()
+    return sig
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_bytes(c, op):
+    """Compulsory bytes per (det, sample) of an operation (map of
+    3 x ny x nx float64)."""
+    n_det, n_time = c["n_det"], c["n_time"]
+    N = n_det * n_time
+    npix = c["shape"][0] * c["shape"][1]
+    bore = 32. / n_det
+    dets = 16. / n_time
+    if op == "to_map":
+        return 4. + bore + dets + 16. * 3 * npix / N
+    if op == "from_map":
+        return 8. + bore + dets + 8. * 3 * npix / N   # signal read + write
+    if op == "to_weight_map":
+        return bore + dets + 16. * 6 * npix / N
+    raise ValueError(op)
+
+
+# ---------------------------------------------------------------------------
+# Our implementation.
+
+def run_ours(args, c, rank, world):
+    import torch
+    import so3g_gb300
+    from so3g_gb300 import _abi
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    lib = _abi.lib()
+    p, q, dets, resp = host_inputs(c)
+    eng = p.get_ProjEng("TQU")
+    q_d = torch.from_numpy(q).to(dev)
+    dets_d = torch.from_numpy(dets).to(dev)
+    resp_d = torch.from_numpy(resp).to(dev)
+    sig = make_signal(torch, c, dev, seed=rank)
+    ny, nx = c["shape"]
+    m = torch.zeros((3, ny, nx), dtype=torch.float64, device=dev)
+    w = torch.zeros((3, 3, ny, nx), dtype=torch.float64, device=dev)
+    out = torch.zeros_like(sig)
+    N = c["n_det"] * c["n_time"]
+    ops = args.ops.split(",")
+    stream = torch.cuda.current_stream()
+
+    def step(accum, ev=None):
+        t = {}
+        if "to_map" in ops:
+            m.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            eng.to_map(m, q_d, dets_d, resp_d, sig, None, None, accum=accum)
+            e1.record(stream)
+            t["to_map"] = (e0, e1)
+        if "from_map" in ops:
+            out.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            eng.from_map(m, q_d, dets_d, resp_d, out)
+            e1.record(stream)
+            t["from_map"] = (e0, e1)
+        return t
+
+    def timed(accum, steps, warmup):
+        for _ in range(warmup):
+            step(accum)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        n0 = lib.so3g_launch_count()
+        e_start = torch.cuda.Event(enable_timing=True)
+        e_end = torch.cuda.Event(enable_timing=True)
+        per = {op: [] for op in ops}
+        with ClockSampler(dev.index) as clk:
+            e_start.record(stream)
+            for _ in range(steps):
+                t = step(accum)
+                for op, ev in t.items():
+                    per[op].append(ev)
+            e_end.record(stream)
+            torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        launches = lib.so3g_launch_count() - n0
+        total_ms = e_start.elapsed_time(e_end)
+        op_ms = {op: float(np.mean([a.elapsed_time(b) for a, b in v])) for op, v in per.items()}
+        return total_ms / steps, op_ms, launches, clk.summary()
+
+    ms, op_ms, launches, clocks = timed(_abi.ACCUM_WARP_RUNS, args.steps, args.warmup)
+    if world > 1:
+        t = torch.tensor([ms], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    res = {"ms_per_step": ms, "op_ms": op_ms, "launches": launches, "clocks": clocks}
+    if not args.no_fp64_path and world == 1:
+        ms64, op64, _, _ = timed(_abi.ACCUM_ATOMIC, max(1, args.steps // 2), 1)
+        res["fp64_path"] = {"ms_per_step": ms64, "op_ms": op64}
+    # to_weight_map, timed on its own (not part of the step).
+    if world == 1:
+        for _ in range(2):
+            w.zero_()
+            eng.to_weight_map(w, q_d, dets_d, resp_d, None, None)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        eng.to_weight_map(w, q_d, dets_d, resp_d, None, None)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        res["to_weight_map_ms"] = e0.elapsed_time(e1)
+    if not args.no_e2e and world == 1:
+        res["e2e"] = run_e2e(args, c, eng, q, dets, resp, sig, dev)
+    del sig, out
+    return res, N
+
+
+def run_e2e(args, c, eng, q, dets, resp, sig_dev, dev):
+    """Same step through the public API with pinned host buffers."""
+    import torch
+    sig_h = torch.empty(sig_dev.shape, dtype=torch.float32, pin_memory=True)
+    sig_h.copy_(sig_dev)
+    out_h = torch.zeros(sig_dev.shape, dtype=torch.float32, pin_memory=True)
+    q_h = torch.from_numpy(q).pin_memory()
+    d_h = torch.from_numpy(dets).pin_memory()
+    r_h = torch.from_numpy(resp).pin_memory()
+    ny, nx = c["shape"]
+    m_h = torch.zeros((3, ny, nx), dtype=torch.float64).pin_memory()
+
+    def step():
+        m_h.zero_()
+        eng.to_map(m_h, q_h, d_h, r_h, sig_h, None, None)
+        out_h.zero_()
+        eng.from_map(m_h, q_h, d_h, r_h, out_h)
+
+    for _ in range(max(1, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    steps = max(1, args.steps // 2)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / steps
+    N = c["n_det"] * c["n_time"]
+    nb_sig = sig_h.numel() * 4
+    nb_map = m_h.numel() * 8
+    nb_point = q_h.numel() * 8 + d_h.numel() * 8 + r_h.numel() * 4
+    h2d = nb_sig + nb_map + nb_point + nb_sig + nb_map + nb_point
+    d2h = nb_map + nb_sig
+    return {"value": N / dt, "unit": "samples/s", "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "ms_per_step": dt * 1e3}
+
+
+# ---------------------------------------------------------------------------
+# CPU: the oracle (the reference's algorithm restated in C++ with OpenMP).
+
+def cpu_sample(c, n_det_s, n_time_s):
+    s = dict(c)
+    s["n_det"], s["n_time"] = n_det_s, n_time_s
+    return s
+
+
+def run_cpu(c, n_det_s, n_time_s, steps=1, threads=None):
+    """to_map (+ 'simple' thread assignment, reported apart) and from_map
+    of the oracle on a slice of the workload; returns samples/s."""
+    from oracle import Oracle
+    orc = Oracle()
+    nthreads = threads or os.cpu_count() or 1
+    orc.set_threads(nthreads)
+    s = cpu_sample(c, n_det_s, n_time_s)
+    p, q, dets, resp = host_inputs(s)
+    eng = p.get_ProjEng("TQU")
+    pz = eng._pz()
+    rng = np.random.default_rng(0)
+    sig = rng.standard_normal((n_det_s, n_time_s), dtype=np.float32)
+    ny, nx = c["shape"]
+    t0 = time.perf_counter()
+    lab = orc.labels(pz, q, dets, 0, nthreads)
+    t_assign = time.perf_counter() - t0
+    threads_ranges = _labels_to_threads(lab, nthreads)
+    best = None
+    for _ in range(steps):
+        m = np.zeros(3 * ny * nx)
+        t0 = time.perf_counter()
+        orc.to_map(pz, q, dets, resp, sig, None, m, threads=threads_ranges)
+        t1 = time.perf_counter()
+        out = np.zeros((n_det_s, n_time_s), np.float32)
+        orc.from_map(pz, q, dets, resp, m, out)
+        t2 = time.perf_counter()
+        if best is None or (t2 - t0) < best[0]:
+            best = (t2 - t0, t1 - t0, t2 - t1)
+    N = n_det_s * n_time_s
+    return {"value": N / best[0], "to_map_s": best[1], "from_map_s": best[2],
+            "assign_s": t_assign, "threads": nthreads, "samples": N,
+            "sample": "%d det x %d samples of the %s workload" % (n_det_s, n_time_s, "same")}
+
+
+class _R:
+    """Minimal Ranges view for oracle.schedule()."""
+
+    def __init__(self, iv):
+        self.iv = iv
+        self.count = 0
+
+    def ranges(self):
+        return np.asarray(self.iv, dtype=np.int32).reshape(-1, 2)
+
+
+def _labels_to_threads(lab, n_domain):
+    """Per-sample stripe labels -> [parallel bunch, serial bunch] of
+    per-thread, per-detector interval lists (pixel_ranges'
+    construction, src/Projection.cxx:1507-1523)."""
+    n_det, n_time = lab.shape
+    par = [[[] for _ in range(n_det)] for _ in range(n_domain)]
+    ser = [[[] for _ in range(n_det)]]
+    for d in range(n_det):
+        row = lab[d]
+        edges = np.flatnonzero(np.diff(row)) + 1
+        starts = np.concatenate([[0], edges])
+        ends = np.concatenate([edges, [n_time]])
+        for a, b in zip(starts, ends):
+            L = row[a]
+            if L < 0:
+                continue
+            (par[L] if L < n_domain else ser[0])[d].append((a, b))
+    return [[[_R(iv) for iv in th] for th in par], [[_R(iv) for iv in th] for th in ser]]
+
+
+def cpu_sample_size(c):
+    # About 10-30 s of CPU work across to_map + from_map.
+    n_det = min(c["n_det"], 100)
+    n_time = min(c["n_time"], 200_000)
+    return n_det, n_time
+
+
+# ---------------------------------------------------------------------------
+
+def main():
+    args = parse()
+    c = config(args)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        dist.init_process_group("nccl")
+    workload = "CAR TQU NonTiled %dx%d float64 map, %d det x %d samples" % (
+        c["shape"][0], c["shape"][1], c["n_det"], c["n_time"])
+    cfg = {"workload": workload, "n_det": c["n_det"], "n_time": c["n_time"],
+           "map": [3] + list(c["shape"]), "step": args.ops.replace(",", " + "),
+           "l2": "inputs larger than L2 (TOD %.1f GB)" % (c["n_det"] * c["n_time"] * 4 / 1e9),
+           "precision": "float64 pointing, float32 products, float64 map accumulation",
+           "parallelism": "replicas" if world > 1 else "single GPU"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        nd, nt = cpu_sample_size(c)
+        r = run_cpu(c, nd, nt, steps=max(1, args.steps))
+        line = {"metric": METRIC, "value": r["value"], "unit": "samples/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step":
+                c["n_det"] * c["n_time"] / r["value"] * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": cfg, "impl": "reference",
+                "cpu_baseline": {"value": r["value"], "unit": "samples/s",
+                                 "cores": r["threads"], "kind": "port",
+                                 "sample": r["sample"] + "; to_map with 'simple' thread "
+                                 "assignment (assignment %.2f s, not timed)" % r["assign_s"]},
+                "e2e": {"value": r["value"], "unit": "samples/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    res, N = run_ours(args, c, rank, world)
+    if rank != 0:
+        return
+    hbm, kind = peaks()
+    ms = res["ms_per_step"]
+    value = N * world / (ms * 1e-3)
+    op = "to_map" if "to_map" in res["op_ms"] else list(res["op_ms"])[0]
+    B = algorithmic_bytes(c, op)
+    achieved = B * N / (res["op_ms"][op] * 1e-3) / 1e9
+    line = {"metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": cfg,
+            "op_ms": res["op_ms"],
+            "roofline": {"bound": "hbm", "kernel": op, "achieved": achieved, "peak": hbm,
+                         "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                         "bytes_per_sample": B, "peak_kind": kind},
+            "clocks": res["clocks"], "gpu_launches": int(res["launches"])}
+    if "fp64_path" in res:
+        f = res["fp64_path"]
+        line["fp64_path"] = {"value": N / (f["ms_per_step"] * 1e-3), "op_ms": f["op_ms"],
+                             "mixed_over_fp64": f["ms_per_step"] / ms}
+    if "to_weight_map_ms" in res:
+        line["to_weight_map"] = {"ms": res["to_weight_map_ms"],
+                                 "samples_per_s": N / (res["to_weight_map_ms"] * 1e-3)}
+    if "e2e" in res:
+        line["e2e"] = res["e2e"]
+    if world == 1 and not args.no_cpu:
+        nd, nt = cpu_sample_size(c)
+        r = run_cpu(c, nd, nt)
+        line["cpu_baseline"] = {"value": r["value"], "unit": "samples/s", "cores": r["threads"],
+                                "kind": "port", "sample": r["sample"] + "; to_map with "
+                                "'simple' thread assignment (assignment not timed)"}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

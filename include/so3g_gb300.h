@@ -1,0 +1,319 @@
+/*
+ * so3g_gb300.h -- C ABI of the GB300 (sm_103a) ProjectionEngine library.
+ *
+ * This is the drop-in boundary for so3g's ProjectionEngine hot path:
+ * quaternion pointing, pixelisation (Flat/Quat/CAR/CEA/ARC/SIN/TAN/ZEA
+ * rectangular maps and HEALPix; NonTiled and Tiled; nearest and bilinear)
+ * and the SpinT/SpinQU/SpinTQU operators to_map, to_weight_map and
+ * from_map.  Every entry point takes plain pointers and sizes; nothing in
+ * a signature is a Python, numpy or torch type.
+ *
+ * Pointer conventions
+ *   - Array arguments of the so3g_proj_* and so3g_precomp_* entry points
+ *     are DEVICE pointers (memory of the current CUDA device), except the
+ *     structs themselves, which live in host memory and are read before the
+ *     call returns.
+ *   - Work is enqueued on `stream` (a cudaStream_t; NULL = legacy default
+ *     stream).  Calls return once the kernels are enqueued; results are
+ *     ordered on the stream.
+ *   - Errors that the host can see (bad arguments) are returned as a
+ *     negative status; so3g_last_error() then holds a message.  Errors that
+ *     only the kernel can see (a sample that lands on an absent tile) are
+ *     recorded in the device error record `err` (4 x int32, see
+ *     so3g_device_error) which the caller zeroes before the call and reads
+ *     after synchronising.
+ *
+ * Layouts (all C-contiguous)
+ *   boresight     (n_time, 4)  float64   quaternion (1,i,j,k) per sample
+ *   dets          (n_det, 4)   float64   detector offset quaternions
+ *   response      (n_det, 2)   float32   (T, P) response per detector
+ *   det_weights   (n_det,)     float32   optional (NULL = all ones)
+ *   signal        n_det rows of n_time float32; row r starts at
+ *                 signal + r * sig_det_stride (elements); unit time stride
+ *   map           see so3g_map
+ *
+ * The reference implementation these entry points replace is the
+ * ProjectionEngine template of so3g, src/Projection.cxx, bound to Python
+ * by the EXPORT_ENGINE macro (src/Projection.cxx:2294-2308).
+ */
+#ifndef SO3G_GB300_H
+#define SO3G_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SO3G_GB300_ABI_VERSION 1
+
+/* Coordinate systems: the CoordSys template parameter (Pointer<C>),
+ * src/Projection.cxx:152-159, 238-507. */
+enum so3g_coord_sys {
+    SO3G_COORD_FLAT = 0,
+    SO3G_COORD_QUAT = 1,
+    SO3G_COORD_CAR  = 2,
+    SO3G_COORD_CEA  = 3,
+    SO3G_COORD_ARC  = 4,
+    SO3G_COORD_SIN  = 5,
+    SO3G_COORD_TAN  = 6,
+    SO3G_COORD_ZEA  = 7
+};
+
+/* Pixel systems: Pixelizor2_Flat (src/Projection.cxx:802-1166) and
+ * Pixelizor_Healpix (src/Projection.cxx:513-800). */
+enum so3g_pix_sys {
+    SO3G_PIX_FLAT    = 0,
+    SO3G_PIX_HEALPIX = 1
+};
+
+/* Interpolation: NearestNeighbor / Bilinear (src/Projection.cxx:166-167). */
+enum so3g_interp {
+    SO3G_INTERP_NEAREST  = 0,
+    SO3G_INTERP_BILINEAR = 1
+};
+
+/* Accumulation strategy of the scatter operators (to_map, to_weight_map). */
+enum so3g_accum {
+    /* One float64 atomic add per (sample, tap, component): the plain
+     * FP64-accumulate path. */
+    SO3G_ACCUM_ATOMIC = 0,
+    /* Runs of equal pixels along a warp's samples are pre-reduced in
+     * registers (compensated float32 two-sum) and flushed with one float64
+     * atomic add per run. */
+    SO3G_ACCUM_WARP_RUNS = 1
+};
+
+/* Status codes returned by every entry point. */
+enum so3g_status {
+    SO3G_OK            = 0,
+    SO3G_ERR_ARGUMENT  = -1,  /* bad argument; message in so3g_last_error() */
+    SO3G_ERR_CUDA      = -2,  /* a CUDA call failed */
+    SO3G_ERR_NOT_INIT  = -3,  /* so3g_init() was not called on this device */
+    SO3G_ERR_RANGE     = -4   /* a size is beyond a documented limit */
+};
+
+/* Device error record codes (err[0]). */
+enum so3g_device_error {
+    SO3G_DEVERR_NONE         = 0,
+    /* A sample landed on a tile that is absent from the map; err[1] is the
+     * smallest such tile index.  Mirrors tiling_exception
+     * (include/exceptions.h:103-116, raised at src/Projection.cxx:1084-1088). */
+    SO3G_DEVERR_MISSING_TILE = 1,
+    /* A precomputed pixel index lies outside its map or tile; err[1] is the
+     * tile (or 0), err[2] the detector and err[3] the sample. */
+    SO3G_DEVERR_PIXEL_RANGE  = 2
+};
+
+/* Pixelisation: the arguments of the ProjEng_* constructor
+ * (Pixelizor2_Flat(bp::object), src/Projection.cxx:821-829 and 971-994;
+ * Pixelizor_Healpix(bp::object), src/Projection.cxx:534-542 and 640-675)
+ * plus the template choices of the class name. */
+typedef struct so3g_pixelization {
+    int32_t coord_sys;      /* enum so3g_coord_sys */
+    int32_t pix_sys;        /* enum so3g_pix_sys */
+    int32_t tiled;          /* 0 = NonTiled, 1 = Tiled */
+    int32_t interp;         /* enum so3g_interp (HEALPix: nearest only) */
+    int32_t n_comp;         /* 1 = SpinT, 2 = SpinQU, 3 = SpinTQU */
+    int32_t naxis[2];       /* Flat: (ny, nx) */
+    int32_t tile_shape[2];  /* Flat Tiled: (tile_ny, tile_nx) */
+    int32_t nside;          /* HEALPix nside */
+    int32_t nest;           /* HEALPix: 1 = NEST, 0 = RING */
+    int32_t nside_tile;     /* HEALPix Tiled */
+    double  cdelt[2];       /* Flat: (dy, dx), radians per pixel */
+    double  crpix[2];       /* Flat: (crpix_y, crpix_x), FITS 1-based */
+} so3g_pixelization;
+
+/* A map, or a weight map.  Untiled: `data` holds (n_comp, <pixels>)
+ * (to_map/from_map) or (n_comp, n_comp, <pixels>) (to_weight_map), where
+ * <pixels> is (ny, nx) for Flat and (12*nside^2,) for HEALPix.
+ * Tiled: tile t holds the same layout over its own pixels, starting at
+ * data + tile_offset[t] (elements); tile_offset[t] < 0 marks an absent tile.
+ * Flat tiles at the right/bottom edge are cropped to the parent map, as
+ * in Pixelizor2_Flat<Tiled>::zeros (src/Projection.cxx:1014-1025). */
+typedef struct so3g_map {
+    double        *data;
+    const int64_t *tile_offset;  /* device array of n_tile, or NULL (untiled) */
+    int32_t        n_tile;       /* number of tiles (0 for untiled) */
+    int32_t        _pad;
+} so3g_map;
+
+/* Sample ranges: the thread_intervals argument (derive_ranges,
+ * src/Projection.cxx:1856-1922) flattened to segments.  Segment k covers
+ * samples [seg[3k+1], seg[3k+2]) of detector seg[3k].  A sample covered
+ * by two segments is projected twice, as in the reference.  NULL means
+ * every sample of every detector once. */
+typedef struct so3g_ranges {
+    const int32_t *seg;   /* device array of n_seg * 3 int32 */
+    int32_t        n_seg;
+    int32_t        max_len;  /* longest segment (end - start) */
+} so3g_ranges;
+
+/* ---- Library state ------------------------------------------------------ */
+
+/* Builds the 16384-entry asin/atan2 interpolation tables on the host (as
+ * the reference's static asinTable/atan2Table, src/Projection.cxx:34-40,
+ * include/so_linterp.h:32-71) and uploads them to the current device.
+ * Must be called once per device before any so3g_proj_* call. */
+int so3g_init(void);
+
+/* Message of the last failing call in this thread ("" if none). */
+const char *so3g_last_error(void);
+
+/* ABI version (SO3G_GB300_ABI_VERSION). */
+int so3g_abi_version(void);
+
+/* Copies the host trig tables (2 x 16384 float64: asin then atan2). */
+int so3g_get_trig_tables(double *asin_vals, double *atan2_vals, int32_t n);
+
+/* Number of kernel launches this library has enqueued since load. */
+int64_t so3g_launch_count(void);
+
+/* ---- Pointing-only queries ----------------------------------------------- */
+
+/* ProjectionEngine::coords (src/Projection.cxx:1316-1349).
+ * coords: (n_det, n_time, 4) float64. */
+int so3g_proj_coords(const so3g_pixelization *pz,
+                     const double *boresight, int32_t n_time,
+                     const double *dets, int32_t n_det,
+                     double *coords, void *stream);
+
+/* ProjectionEngine::pixels (src/Projection.cxx:1351-1385).
+ * pixel: (n_det, n_time, index_count) int32, index_count = 2 (Flat),
+ * 3 (Flat Tiled), 1 (HEALPix), 2 (HEALPix Tiled).  Off-map samples get -1
+ * in slot 0 and keep the previous sample's other slots, as the reference. */
+int so3g_proj_pixels(const so3g_pixelization *pz,
+                     const double *boresight, int32_t n_time,
+                     const double *dets, int32_t n_det,
+                     int32_t *pixel, void *stream);
+
+/* ProjectionEngine::pointing_matrix (src/Projection.cxx:1391-1438).
+ * pixel as so3g_proj_pixels; proj: (n_det, n_time, n_comp) float32. */
+int so3g_proj_pointing_matrix(const so3g_pixelization *pz,
+                              const double *boresight, int32_t n_time,
+                              const double *dets, int32_t n_det,
+                              const float *response,
+                              int32_t *pixel, float *proj, void *stream);
+
+/* ProjectionEngine::tile_hits (src/Projection.cxx:1543-1601).
+ * hits: (n_tile,) int64, zeroed by the caller; counts every interpolation
+ * tap of every sample (the reference counts in int; int64 cannot wrap). */
+int so3g_proj_tile_hits(const so3g_pixelization *pz,
+                        const double *boresight, int32_t n_time,
+                        const double *dets, int32_t n_det,
+                        int64_t *hits, int32_t n_tile, void *stream);
+
+/* Domain changes behind ProjectionEngine::pixel_ranges
+ * (src/Projection.cxx:1440-1541) and ::tile_ranges (:1606-1705).  Every
+ * sample gets a domain label:
+ *   mode 0: stripe(pixel, n_domain)  (pixel_ranges with map = None)
+ *   mode 1: (int) dmap[pixel]        (pixel_ranges with a map; dmap holds
+ *           the map's first component, laid out as so3g_map)
+ *   mode 2: tile_domain[tile]        (tile_ranges; tile_domain is a device
+ *           array of n_tile entries, -1 = unassigned)
+ * with -1 for a sample with no pixel and n_domain for one whose
+ * interpolation taps disagree.  For every sample t whose label differs from
+ * that of sample t-1 (and for t = 0) one edge record (det, t, label) of 3
+ * int32 is appended to `edges` (capacity max_edges records, unordered).
+ * n_edges (device int64, zeroed by the caller) receives the number of
+ * edges; when it exceeds max_edges the extra records are dropped and the
+ * caller retries with more room.  A run of equal labels >= 0 from one edge
+ * to the next is one interval of the reference's ranges. */
+int so3g_proj_domain_edges(const so3g_pixelization *pz,
+                           const double *boresight, int32_t n_time,
+                           const double *dets, int32_t n_det,
+                           int32_t mode, int32_t n_domain,
+                           const so3g_map *dmap,
+                           const int32_t *tile_domain, int32_t n_tile,
+                           int32_t *edges, int64_t max_edges,
+                           int64_t *n_edges, int32_t *err, void *stream);
+
+/* ---- Projection operators ------------------------------------------------ */
+
+/* ProjectionEngine::to_map (src/Projection.cxx:1924-1966, inner loop
+ * to_map_single_thread :1772-1811):
+ *   map[c, pix] += sig * pf[c] * w * det_wt   (float32 product, float64 sum)
+ * Detectors with det_weights == 0 are skipped.  ranges may be NULL. */
+int so3g_proj_to_map(const so3g_pixelization *pz,
+                     const double *boresight, int32_t n_time,
+                     const double *dets, int32_t n_det,
+                     const float *response,
+                     const float *signal, int64_t sig_det_stride,
+                     const float *det_weights,
+                     const so3g_ranges *ranges,
+                     const so3g_map *map,
+                     int32_t accum, int32_t *err, void *stream);
+
+/* ProjectionEngine::to_weight_map (src/Projection.cxx:1968-2010, inner
+ * loop :1813-1854): W[i, j, pix] += pf[i]*pf[j]*w*w*det_wt for j >= i. */
+int so3g_proj_to_weight_map(const so3g_pixelization *pz,
+                            const double *boresight, int32_t n_time,
+                            const double *dets, int32_t n_det,
+                            const float *response,
+                            const float *det_weights,
+                            const so3g_ranges *ranges,
+                            const so3g_map *map,
+                            int32_t accum, int32_t *err, void *stream);
+
+/* ProjectionEngine::from_map (src/Projection.cxx:1728-1770):
+ *   sig += map[c, pix] * pf[c] * w, rounded to float32 after every term;
+ * accumulates into `signal`. */
+int so3g_proj_from_map(const so3g_pixelization *pz,
+                       const double *boresight, int32_t n_time,
+                       const double *dets, int32_t n_det,
+                       const float *response,
+                       const so3g_map *map,
+                       float *signal, int64_t sig_det_stride,
+                       int32_t *err, void *stream);
+
+/* ---- Precomputed pointing (ProjEng_Precomp, src/Projection.cxx:2012-2256) -
+ * pixel: (n_det, n_time, n_index) int32 with a close-packed last axis;
+ * n_index is 2 for NonTiled (iy, ix) and 3 for Tiled (tile, iy, ix).
+ * Samples with pixel[..., 0] < 0 are skipped.  spin_proj: (n_det, n_time,
+ * n_comp) float32.  The map is (n_comp, ny, nx) (weight map: (n_comp,
+ * n_comp, ny, nx)); a tiled map is so3g_map's tile list, tile t being
+ * (.., tile_dims[2t], tile_dims[2t+1]).  A pixel outside its map or tile
+ * is skipped and recorded as SO3G_DEVERR_PIXEL_RANGE (the reference does
+ * not check it).  */
+typedef struct so3g_precomp_geom {
+    int32_t        tiled;
+    int32_t        n_comp;
+    int32_t        naxis[2];    /* untiled map (ny, nx) */
+    const int32_t *tile_dims;   /* tiled: device array (n_tile, 2) */
+} so3g_precomp_geom;
+
+/* ProjEng_Precomp::to_map (src/Projection.cxx:2087-2122, 2157-2206):
+ *   map[c, pix] += det_wt * sig * pf[c]   (float32 product, float64 sum) */
+int so3g_precomp_to_map(const so3g_precomp_geom *g,
+                        const int32_t *pixel, const float *spin_proj,
+                        int32_t n_det, int32_t n_time,
+                        const float *signal, int64_t sig_det_stride,
+                        const float *det_weights,
+                        const so3g_ranges *ranges,
+                        const so3g_map *map,
+                        int32_t accum, int32_t *err, void *stream);
+
+/* ProjEng_Precomp::to_weight_map (src/Projection.cxx:2124-2155, 2208-2253):
+ *   W[i, j, pix] += pf[i] * pf[j] * det_wt for j >= i. */
+int so3g_precomp_to_weight_map(const so3g_precomp_geom *g,
+                               const int32_t *pixel, const float *spin_proj,
+                               int32_t n_det, int32_t n_time,
+                               const float *det_weights,
+                               const so3g_ranges *ranges,
+                               const so3g_map *map,
+                               int32_t accum, int32_t *err, void *stream);
+
+/* ProjEng_Precomp::from_map (src/Projection.cxx:2036-2085):
+ *   sig += sum_c pf[c] * map[c, pix]  (the sum over c in float32) */
+int so3g_precomp_from_map(const so3g_precomp_geom *g,
+                          const int32_t *pixel, const float *spin_proj,
+                          int32_t n_det, int32_t n_time,
+                          const so3g_map *map,
+                          float *signal, int64_t sig_det_stride,
+                          int32_t *err, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SO3G_GB300_H */

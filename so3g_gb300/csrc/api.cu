@@ -1,0 +1,189 @@
+// api.cu -- library state of the C ABI: trig tables per device, error
+// reporting, launch accounting and pixelization validation.
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <atomic>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "host.h"
+
+namespace so3g {
+
+namespace {
+
+thread_local std::string t_err;
+std::atomic<long long> g_launches{0};
+std::mutex g_mu;
+constexpr int kMaxDevices = 64;
+double *g_lut[kMaxDevices] = {nullptr};
+std::vector<double> g_host_lut;
+
+// asinTable / atan2Table construction (include/so_linterp.h:35-39, 51-56),
+// with the host math library, as the reference's static tables
+// (src/Projection.cxx:36-38).
+void build_host_tables() {
+    if (!g_host_lut.empty()) return;
+    g_host_lut.resize(2 * kLutN);
+    const double dx = 1. / (kLutN - 1);
+    for (int i = 0; i < kLutN; i++) g_host_lut[i] = std::asin(i * dx);
+    for (int i = 0; i < kLutN; i++) g_host_lut[kLutN + i] = std::atan2(i * dx, 1.);
+}
+
+bool pow2(long long v) { return v > 0 && (v & (v - 1)) == 0; }
+
+}  // namespace
+
+int set_error(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    t_err = buf;
+    return code;
+}
+
+void clear_error() { t_err.clear(); }
+
+int after_launch(const char *what) {
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return set_error(SO3G_ERR_CUDA, "%s: launch failed: %s", what, cudaGetErrorString(e));
+    return SO3G_OK;
+}
+
+const double *device_lut() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
+    return g_lut[dev];
+}
+
+int pix_kind(const so3g_pixelization *pz) {
+    if (pz->pix_sys == SO3G_PIX_HEALPIX) return pz->tiled ? PX_HP_T : PX_HP_NT;
+    return (pz->tiled ? 2 : 0) + (pz->interp == SO3G_INTERP_BILINEAR ? 1 : 0);
+}
+
+int make_geom(const so3g_pixelization *pz, DGeom *g) {
+    if (!pz) return set_error(SO3G_ERR_ARGUMENT, "pixelization is NULL");
+    std::memset(g, 0, sizeof(*g));
+    if (pz->n_comp < 1 || pz->n_comp > 3)
+        return set_error(SO3G_ERR_ARGUMENT, "n_comp must be 1, 2 or 3 (got %d)", pz->n_comp);
+    if (pz->coord_sys < SO3G_COORD_FLAT || pz->coord_sys > SO3G_COORD_ZEA)
+        return set_error(SO3G_ERR_ARGUMENT, "unknown coordinate system %d", pz->coord_sys);
+    if (pz->interp != SO3G_INTERP_NEAREST && pz->interp != SO3G_INTERP_BILINEAR)
+        return set_error(SO3G_ERR_ARGUMENT, "unknown interpolation %d", pz->interp);
+    g->ncomp = pz->n_comp;
+    g->lut = device_lut();
+    if (!g->lut) return set_error(SO3G_ERR_NOT_INIT, "so3g_init() was not called on this device");
+    if (pz->pix_sys == SO3G_PIX_HEALPIX) {
+        if (pz->coord_sys != SO3G_COORD_CAR)
+            return set_error(SO3G_ERR_ARGUMENT, "HEALPix pixelization needs CAR coordinates");
+        if (pz->interp != SO3G_INTERP_NEAREST)
+            return set_error(SO3G_ERR_ARGUMENT, "HEALPix supports nearest interpolation only");
+        // check_nside, src/Projection.cxx:607-614
+        if (!(pz->nside > 0 && pz->nside < 8192 && pow2(pz->nside)))
+            return set_error(SO3G_ERR_ARGUMENT, "Invalid nside %d", pz->nside);
+        g->nside = pz->nside;
+        g->npix = 12LL * pz->nside * pz->nside;
+        g->nest = pz->nest ? 1 : 0;
+        if (pz->tiled) {
+            if (!pz->nest) return set_error(SO3G_ERR_ARGUMENT, "RING not supported for tiled maps");
+            if (!(pz->nside_tile > 0 && pz->nside_tile < 8192 && pow2(pz->nside_tile)))
+                return set_error(SO3G_ERR_ARGUMENT, "Invalid nside %d", pz->nside_tile);
+            if (pz->nside_tile > pz->nside)
+                return set_error(SO3G_ERR_ARGUMENT, "Invalid nside_tile %d > nside %d",
+                                 pz->nside_tile, pz->nside);
+            g->n_tile = (int)(12LL * pz->nside_tile * pz->nside_tile);
+            g->nppt = g->npix / g->n_tile;
+        }
+        return SO3G_OK;
+    }
+    if (pz->pix_sys != SO3G_PIX_FLAT)
+        return set_error(SO3G_ERR_ARGUMENT, "unknown pixel system %d", pz->pix_sys);
+    if (pz->naxis[0] < 0 || pz->naxis[1] < 0)
+        return set_error(SO3G_ERR_ARGUMENT, "negative map shape");
+    g->ny = pz->naxis[0];
+    g->nx = pz->naxis[1];
+    g->cdy = pz->cdelt[0];
+    g->cdx = pz->cdelt[1];
+    g->cry = pz->crpix[0];
+    g->crx = pz->crpix[1];
+    if (pz->tiled) {
+        if (pz->tile_shape[0] <= 0 || pz->tile_shape[1] <= 0)
+            return set_error(SO3G_ERR_ARGUMENT, "tile shape must be positive");
+        g->ty = pz->tile_shape[0];
+        g->tx = pz->tile_shape[1];
+        g->nty = (g->ny + g->ty - 1) / g->ty;
+        g->ntx = (g->nx + g->tx - 1) / g->tx;
+        g->n_tile = g->nty * g->ntx;
+        if (g->ntx == 0) g->ntx = 1;  // empty map: keeps the tile arithmetic defined
+    }
+    return SO3G_OK;
+}
+
+int attach_map(const so3g_pixelization *pz, const so3g_map *m, DGeom *g) {
+    if (!m || !m->data) return set_error(SO3G_ERR_ARGUMENT, "map is NULL");
+    if (pz->tiled) {
+        if (!m->tile_offset)
+            return set_error(SO3G_ERR_ARGUMENT, "tiled map needs a tile_offset table");
+        if (m->n_tile != g->n_tile)
+            return set_error(SO3G_ERR_ARGUMENT, "tiled map has %d tiles; the pixelization has %d",
+                             m->n_tile, g->n_tile);
+        g->tile_offset = reinterpret_cast<const long long *>(m->tile_offset);
+        g->n_tile_map = m->n_tile;
+    }
+    return SO3G_OK;
+}
+
+}  // namespace so3g
+
+using namespace so3g;
+
+extern "C" {
+
+int so3g_abi_version(void) { return SO3G_GB300_ABI_VERSION; }
+
+const char *so3g_last_error(void) { return t_err.c_str(); }
+
+int64_t so3g_launch_count(void) { return (int64_t)g_launches.load(); }
+
+int so3g_init(void) {
+    clear_error();
+    std::lock_guard<std::mutex> lk(g_mu);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_error(SO3G_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+    if (dev < 0 || dev >= kMaxDevices) return set_error(SO3G_ERR_RANGE, "device %d out of range", dev);
+    build_host_tables();
+    if (g_lut[dev]) return SO3G_OK;
+    double *d = nullptr;
+    e = cudaMalloc(&d, sizeof(double) * 2 * kLutN);
+    if (e != cudaSuccess) return set_error(SO3G_ERR_CUDA, "cudaMalloc: %s", cudaGetErrorString(e));
+    e = cudaMemcpy(d, g_host_lut.data(), sizeof(double) * 2 * kLutN, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return set_error(SO3G_ERR_CUDA, "cudaMemcpy: %s", cudaGetErrorString(e));
+    }
+    g_lut[dev] = d;
+    return SO3G_OK;
+}
+
+int so3g_get_trig_tables(double *asin_vals, double *atan2_vals, int32_t n) {
+    clear_error();
+    if (n != kLutN) return set_error(SO3G_ERR_ARGUMENT, "table size is %d", kLutN);
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        build_host_tables();
+    }
+    std::memcpy(asin_vals, g_host_lut.data(), sizeof(double) * kLutN);
+    std::memcpy(atan2_vals, g_host_lut.data() + kLutN, sizeof(double) * kLutN);
+    return SO3G_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,68 @@
+// host.h -- host-side helpers shared by the translation units of the C ABI.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "../../include/so3g_gb300.h"
+#include "device.cuh"
+
+namespace so3g {
+
+// Records `msg` as this thread's last error and returns `code`.
+int set_error(int code, const char *fmt, ...);
+// Clears the last error (each entry point starts with it).
+void clear_error();
+// Checks cudaGetLastError() after a launch; counts the launch.
+int after_launch(const char *what);
+// Per-device trig table (asin then atan2, 2 x kLutN float64), or NULL.
+const double *device_lut();
+
+// Validates a pixelization and fills the device geometry (without the map).
+int make_geom(const so3g_pixelization *pz, DGeom *g);
+// Adds the map's tile table to the geometry; checks the tile count.
+int attach_map(const so3g_pixelization *pz, const so3g_map *m, DGeom *g);
+// Pixelizor kind (PX_*) of a pixelization.
+int pix_kind(const so3g_pixelization *pz);
+
+// Block and piece sizes of the per-segment projection kernels.
+constexpr int kBlock = 256;
+constexpr int kMinPiece = 4096;
+
+// Piece length so that no segment needs more than 65535 pieces.
+inline int piece_len(long long max_len) {
+    long long p = kMinPiece;
+    while ((max_len + p - 1) / p > 65535) p *= 2;
+    return (int)p;
+}
+
+// Launch dispatch over (coordinate system, pixelizor): F is a functor with
+// a templated operator()<C, P>() returning int.
+template <class F>
+int dispatch_cp(int coord, int kind, F &&f) {
+#define SO3G_P(C)                                                   \
+    switch (kind) {                                                  \
+    case PX_FLAT_NT_NN: return f.template run<C, PX_FLAT_NT_NN>();   \
+    case PX_FLAT_NT_BL: return f.template run<C, PX_FLAT_NT_BL>();   \
+    case PX_FLAT_T_NN: return f.template run<C, PX_FLAT_T_NN>();     \
+    case PX_FLAT_T_BL: return f.template run<C, PX_FLAT_T_BL>();     \
+    default: break;                                                  \
+    }
+    if (kind == PX_HP_NT) return f.template run<SO3G_COORD_CAR, PX_HP_NT>();
+    if (kind == PX_HP_T) return f.template run<SO3G_COORD_CAR, PX_HP_T>();
+    switch (coord) {
+    case SO3G_COORD_FLAT: SO3G_P(SO3G_COORD_FLAT) break;
+    case SO3G_COORD_QUAT: SO3G_P(SO3G_COORD_QUAT) break;
+    case SO3G_COORD_CAR: SO3G_P(SO3G_COORD_CAR) break;
+    case SO3G_COORD_CEA: SO3G_P(SO3G_COORD_CEA) break;
+    case SO3G_COORD_ARC: SO3G_P(SO3G_COORD_ARC) break;
+    case SO3G_COORD_SIN: SO3G_P(SO3G_COORD_SIN) break;
+    case SO3G_COORD_TAN: SO3G_P(SO3G_COORD_TAN) break;
+    case SO3G_COORD_ZEA: SO3G_P(SO3G_COORD_ZEA) break;
+    default: break;
+    }
+#undef SO3G_P
+    return set_error(SO3G_ERR_ARGUMENT, "unsupported coordinate system %d / pixelizor %d",
+                     coord, kind);
+}
+
+}  // namespace so3g

@@ -1,0 +1,280 @@
+// precomp.cu -- ProjEng_Precomp: projection with precomputed pointing
+// (pixel indices and spin projection factors per sample).  No trigonometry:
+// these kernels stream the pointing, the signal and the map and are bound by
+// HBM bandwidth and atomic throughput.
+
+#include "host.h"
+
+namespace so3g {
+
+namespace {
+
+struct PcArgs {
+    int tiled, nc, ny, nx;
+    const int *tile_dims;
+    const long long *tile_offset;
+    int n_tile;
+    const int *pixel;
+    const float *spin;
+    int n_time;
+    const float *signal;
+    float *signal_out;
+    long long sig_stride;
+    const float *det_weights;
+    Segs segs;
+    int piece;
+    int accum;
+    int *err;
+    double *map;
+};
+
+// Element offset and plane size of a precomputed pixel tuple; false if it
+// is skipped (the error record says why).
+template <bool TILED>
+__device__ __forceinline__ bool pc_locate(const PcArgs &a, const int *p, int det, int t,
+                                          long long *off, long long *plane) {
+    if (!TILED) {
+        // Pixelizor2_Flat<NonTiled>::pix, src/Projection.cxx:881-886
+        if (p[0] >= a.ny || p[1] < 0 || p[1] >= a.nx) {
+            record_pixel_range(a.err, 0, det, t);
+            return false;
+        }
+        *off = (long long)p[0] * a.nx + p[1];
+        *plane = (long long)a.ny * a.nx;
+        return true;
+    }
+    // Pixelizor2_Flat<Tiled>::pix, src/Projection.cxx:1084-1093
+    const int tile = p[0];
+    long long toff = tile < a.n_tile ? __ldg(a.tile_offset + tile) : -1;
+    if (toff < 0) {
+        record_missing_tile(a.err, tile);
+        return false;
+    }
+    const int tny = __ldg(a.tile_dims + 2 * tile), tnx = __ldg(a.tile_dims + 2 * tile + 1);
+    if (p[1] < 0 || p[1] >= tny || p[2] < 0 || p[2] >= tnx) {
+        record_pixel_range(a.err, tile, det, t);
+        return false;
+    }
+    *off = toff + (long long)p[1] * tnx + p[2];
+    *plane = (long long)tny * tnx;
+    return true;
+}
+
+template <bool TILED>
+__device__ __forceinline__ void load_tuple(const PcArgs &a, long long s, int *p) {
+    if (!TILED) {
+        int2 v = __ldg(reinterpret_cast<const int2 *>(a.pixel) + s);
+        p[0] = v.x;
+        p[1] = v.y;
+    } else {
+        const int *q = a.pixel + 3 * s;
+        p[0] = __ldg(q);
+        p[1] = __ldg(q + 1);
+        p[2] = __ldg(q + 2);
+    }
+}
+
+template <bool TILED, bool WEIGHT>
+__global__ void __launch_bounds__(kBlock) k_pc_scatter(PcArgs a) {
+    int det, t0, t1;
+    if (!seg_piece(a.segs, a.piece, det, t0, t1)) return;
+    float det_wt = 1.f;
+    if (a.det_weights) {
+        det_wt = __ldg(a.det_weights + det);
+        if (det_wt == 0.f) return;  // src/Projection.cxx:2101-2105
+    }
+    const int nc = a.nc;
+    const int lane = threadIdx.x & 31;
+    constexpr int NV = WEIGHT ? 6 : 3;
+    int mult[NV];
+    unsigned vmask = 0;
+    if (!WEIGHT) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            mult[c] = c;
+            if (c < nc) vmask |= 1u << c;
+        }
+    } else {
+        int k = 0;
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = i; j < 3; j++, k++) {
+                mult[k] = i * nc + j;
+                if (i < nc && j < nc) vmask |= 1u << k;
+            }
+    }
+    for (int base = t0 + (threadIdx.x & ~31); base < t1; base += blockDim.x) {
+        const int t = base + lane;
+        long long off = -1, plane = 0;
+        float v[NV];
+#pragma unroll
+        for (int k = 0; k < NV; k++) v[k] = 0.f;
+        if (t < t1) {
+            const long long s = (long long)det * a.n_time + t;
+            int p[3];
+            load_tuple<TILED>(a, s, p);
+            if (p[0] >= 0 && pc_locate<TILED>(a, p, det, t, &off, &plane)) {
+                float pf[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+                for (int c = 0; c < 3; c++)
+                    if (c < nc) pf[c] = __ldg(a.spin + s * nc + c);
+                if (!WEIGHT) {
+                    // src/Projection.cxx:2117
+                    const float sig = __ldg(a.signal + det * a.sig_stride + t);
+#pragma unroll
+                    for (int c = 0; c < 3; c++) v[c] = det_wt * sig * pf[c];
+                } else {
+                    // src/Projection.cxx:2151
+                    int k = 0;
+#pragma unroll
+                    for (int i = 0; i < 3; i++)
+#pragma unroll
+                        for (int j = i; j < 3; j++, k++) v[k] = pf[i] * pf[j] * det_wt;
+                }
+            }
+        }
+        if (a.accum == SO3G_ACCUM_WARP_RUNS) {
+            flush_runs<NV>(off, plane, v, mult, vmask, a.map);
+        } else if (off >= 0) {
+#pragma unroll
+            for (int k = 0; k < NV; k++)
+                if ((vmask >> k) & 1u) atomicAdd(a.map + off + mult[k] * plane, (double)v[k]);
+        }
+    }
+}
+
+template <bool TILED>
+__global__ void __launch_bounds__(kBlock) k_pc_from_map(PcArgs a) {
+    // ProjEng_Precomp::from_map, src/Projection.cxx:2066-2082
+    int det, t0, t1;
+    if (!seg_piece(a.segs, a.piece, det, t0, t1)) return;
+    const int nc = a.nc;
+    for (int t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
+        const long long s = (long long)det * a.n_time + t;
+        int p[3];
+        load_tuple<TILED>(a, s, p);
+        if (p[0] < 0) continue;
+        long long off, plane;
+        if (!pc_locate<TILED>(a, p, det, t, &off, &plane)) continue;
+        float sig = 0;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            if (c < nc) {
+                const float pf = __ldg(a.spin + s * nc + c);
+                sig += pf * __ldg(a.map + off + c * plane);
+            }
+        }
+        a.signal_out[det * a.sig_stride + t] += sig;
+    }
+}
+
+int pc_common(PcArgs &a, const so3g_precomp_geom *g, const int32_t *pixel,
+              const float *spin_proj, int32_t n_det, int32_t n_time, const so3g_map *map) {
+    clear_error();
+    if (!g) return set_error(SO3G_ERR_ARGUMENT, "geometry is NULL");
+    if (g->n_comp < 1 || g->n_comp > 3)
+        return set_error(SO3G_ERR_ARGUMENT, "n_comp must be 1, 2 or 3 (got %d)", g->n_comp);
+    if (n_det < 0 || n_time < 0) return set_error(SO3G_ERR_ARGUMENT, "negative n_det or n_time");
+    if (!map || !map->data) return set_error(SO3G_ERR_ARGUMENT, "map is NULL");
+    a.tiled = g->tiled ? 1 : 0;
+    a.nc = g->n_comp;
+    a.ny = g->naxis[0];
+    a.nx = g->naxis[1];
+    if (a.tiled) {
+        if (!map->tile_offset || !g->tile_dims)
+            return set_error(SO3G_ERR_ARGUMENT, "tiled map needs tile_offset and tile_dims");
+        a.tile_offset = reinterpret_cast<const long long *>(map->tile_offset);
+        a.tile_dims = g->tile_dims;
+        a.n_tile = map->n_tile;
+    }
+    a.pixel = pixel;
+    a.spin = spin_proj;
+    a.n_time = n_time;
+    if (n_det > 0 && n_time > 0 && (!pixel || !spin_proj))
+        return set_error(SO3G_ERR_ARGUMENT, "NULL pixel or spin_proj");
+    return SO3G_OK;
+}
+
+}  // namespace
+
+}  // namespace so3g
+
+using namespace so3g;
+
+extern "C" {
+
+int so3g_precomp_to_map(const so3g_precomp_geom *g, const int32_t *pixel,
+                        const float *spin_proj, int32_t n_det, int32_t n_time,
+                        const float *signal, int64_t sig_det_stride, const float *det_weights,
+                        const so3g_ranges *ranges, const so3g_map *map, int32_t accum,
+                        int32_t *err, void *stream) {
+    PcArgs a{};
+    int rc = pc_common(a, g, pixel, spin_proj, n_det, n_time, map);
+    if (rc) return rc;
+    if (accum != SO3G_ACCUM_ATOMIC && accum != SO3G_ACCUM_WARP_RUNS)
+        return set_error(SO3G_ERR_ARGUMENT, "unknown accumulation mode %d", accum);
+    long long n_seg = ranges ? ranges->n_seg : n_det;
+    long long max_len = ranges ? ranges->max_len : n_time;
+    if (n_seg <= 0 || max_len <= 0 || n_time == 0) return SO3G_OK;
+    if (!signal) return set_error(SO3G_ERR_ARGUMENT, "NULL signal");
+    a.signal = signal;
+    a.sig_stride = sig_det_stride;
+    a.det_weights = det_weights;
+    a.segs = Segs{ranges ? ranges->seg : nullptr, n_time};
+    a.piece = piece_len(max_len);
+    a.accum = accum;
+    a.err = err;
+    a.map = map->data;
+    dim3 grid((unsigned)n_seg, (unsigned)((max_len + a.piece - 1) / a.piece));
+    if (a.tiled) k_pc_scatter<true, false><<<grid, kBlock, 0, (cudaStream_t)stream>>>(a);
+    else k_pc_scatter<false, false><<<grid, kBlock, 0, (cudaStream_t)stream>>>(a);
+    return after_launch("precomp to_map");
+}
+
+int so3g_precomp_to_weight_map(const so3g_precomp_geom *g, const int32_t *pixel,
+                               const float *spin_proj, int32_t n_det, int32_t n_time,
+                               const float *det_weights, const so3g_ranges *ranges,
+                               const so3g_map *map, int32_t accum, int32_t *err, void *stream) {
+    PcArgs a{};
+    int rc = pc_common(a, g, pixel, spin_proj, n_det, n_time, map);
+    if (rc) return rc;
+    if (accum != SO3G_ACCUM_ATOMIC && accum != SO3G_ACCUM_WARP_RUNS)
+        return set_error(SO3G_ERR_ARGUMENT, "unknown accumulation mode %d", accum);
+    long long n_seg = ranges ? ranges->n_seg : n_det;
+    long long max_len = ranges ? ranges->max_len : n_time;
+    if (n_seg <= 0 || max_len <= 0 || n_time == 0) return SO3G_OK;
+    a.det_weights = det_weights;
+    a.segs = Segs{ranges ? ranges->seg : nullptr, n_time};
+    a.piece = piece_len(max_len);
+    a.accum = accum;
+    a.err = err;
+    a.map = map->data;
+    dim3 grid((unsigned)n_seg, (unsigned)((max_len + a.piece - 1) / a.piece));
+    if (a.tiled) k_pc_scatter<true, true><<<grid, kBlock, 0, (cudaStream_t)stream>>>(a);
+    else k_pc_scatter<false, true><<<grid, kBlock, 0, (cudaStream_t)stream>>>(a);
+    return after_launch("precomp to_weight_map");
+}
+
+int so3g_precomp_from_map(const so3g_precomp_geom *g, const int32_t *pixel,
+                          const float *spin_proj, int32_t n_det, int32_t n_time,
+                          const so3g_map *map, float *signal, int64_t sig_det_stride,
+                          int32_t *err, void *stream) {
+    PcArgs a{};
+    int rc = pc_common(a, g, pixel, spin_proj, n_det, n_time, map);
+    if (rc) return rc;
+    if (n_det == 0 || n_time == 0) return SO3G_OK;
+    if (!signal) return set_error(SO3G_ERR_ARGUMENT, "NULL signal");
+    a.signal_out = signal;
+    a.sig_stride = sig_det_stride;
+    a.segs = Segs{nullptr, n_time};
+    a.piece = piece_len(n_time);
+    a.err = err;
+    a.map = map->data;
+    dim3 grid((unsigned)n_det, (unsigned)((n_time + a.piece - 1) / a.piece));
+    if (a.tiled) k_pc_from_map<true><<<grid, kBlock, 0, (cudaStream_t)stream>>>(a);
+    else k_pc_from_map<false><<<grid, kBlock, 0, (cudaStream_t)stream>>>(a);
+    return after_launch("precomp from_map");
+}
+
+}  // extern "C"

@@ -1,0 +1,290 @@
+"""Interval lists: RangesInt32 and RangesMatrix.
+
+RangesInt32 follows the semantics of so3g's Ranges<int32_t>
+(include/Ranges.h:14-65, src/Ranges.cxx): a sample count plus a list of
+half-open [start, end) intervals.  add_interval() merges; the thread
+assignment routines build their lists with append_interval_no_check(),
+which does not.  RangesMatrix follows python/proj/ranges.py:11-297: a
+nested container of Ranges whose last axis is the sample axis.
+
+These are host-side containers (the argument type of ``thread_intervals``),
+kept in numpy; the projection kernels receive them flattened to
+(det, start, end) segments.
+"""
+import numpy as np
+
+
+class RangesInt32:
+    """Half-open intervals over ``count`` samples."""
+
+    def __init__(self, count=0, reference=0):
+        self.count = int(count)
+        self.reference = int(reference)
+        self._segs = []  # list of [start, end]
+
+    # -- construction --------------------------------------------------------
+    @classmethod
+    def from_array(cls, intervals, count):
+        r = cls(count)
+        for a, b in np.asarray(intervals, dtype=np.int64).reshape(-1, 2):
+            r.add_interval(int(a), int(b))
+        return r
+
+    @classmethod
+    def from_mask(cls, mask):
+        mask = np.asarray(mask, dtype=bool)
+        if mask.ndim != 1:
+            return RangesMatrix([cls.from_mask(m) for m in mask])
+        r = cls(len(mask))
+        if len(mask):
+            d = np.diff(np.concatenate([[0], mask.astype(np.int8), [0]]))
+            starts = np.nonzero(d == 1)[0]
+            ends = np.nonzero(d == -1)[0]
+            r._segs = [[int(a), int(b)] for a, b in zip(starts, ends)]
+        return r
+
+    def copy(self):
+        r = RangesInt32(self.count, self.reference)
+        r._segs = [list(s) for s in self._segs]
+        return r
+
+    def zeros_like(self):
+        return RangesInt32(self.count, self.reference)
+
+    def ones_like(self):
+        r = RangesInt32(self.count, self.reference)
+        if self.count > 0:
+            r._segs = [[0, self.count]]
+        return r
+
+    # -- basic operations ------------------------------------------------------
+    def append_interval_no_check(self, start, end):
+        self._segs.append([int(start), int(end)])
+        return self
+
+    def add_interval(self, start, end):
+        start, end = int(start), int(end)
+        self._segs.append([start, end])
+        self._cleanup()
+        return self
+
+    def _cleanup(self):
+        segs = sorted((max(0, a), min(self.count, b)) for a, b in self._segs)
+        out = []
+        for a, b in segs:
+            if b <= a:
+                continue
+            if out and a <= out[-1][1]:
+                out[-1][1] = max(out[-1][1], b)
+            else:
+                out.append([a, b])
+        self._segs = out
+
+    def merge(self, src):
+        self._segs.extend(list(s) for s in src._segs)
+        self._cleanup()
+        return self
+
+    def intersect(self, src):
+        self._segs = (self * src)._segs
+        return self
+
+    def complement(self):
+        out = RangesInt32(self.count, self.reference)
+        x = 0
+        for a, b in sorted(self._segs):
+            if a > x:
+                out._segs.append([x, a])
+            x = max(x, b)
+        if x < self.count:
+            out._segs.append([x, self.count])
+        return out
+
+    def buffer(self, buff):
+        self._segs = [[a - buff, b + buff] for a, b in self._segs]
+        self._cleanup()
+        return self
+
+    def buffered(self, buff):
+        return self.copy().buffer(buff)
+
+    def close_gaps(self, gap):
+        segs = sorted(self._segs)
+        out = []
+        for a, b in segs:
+            if out and a - out[-1][1] <= gap:
+                out[-1][1] = max(out[-1][1], b)
+            else:
+                out.append([a, b])
+        self._segs = out
+        return self
+
+    # -- views -----------------------------------------------------------------
+    def ranges(self):
+        """(n, 2) int32 array of [start, end) pairs."""
+        if not self._segs:
+            return np.zeros((0, 2), dtype=np.int32)
+        return np.array(self._segs, dtype=np.int32).reshape(-1, 2)
+
+    def mask(self):
+        m = np.zeros(self.count, dtype=bool)
+        for a, b in self._segs:
+            m[max(a, 0):max(b, 0)] = True
+        return m
+
+    @property
+    def shape(self):
+        return (self.count,)
+
+    def __len__(self):
+        return self.count
+
+    def __invert__(self):
+        return self.complement()
+
+    def __neg__(self):
+        return self.complement()
+
+    def __add__(self, other):
+        return self.copy().merge(other)
+
+    def __mul__(self, other):
+        out = RangesInt32(self.count, self.reference)
+        a = sorted(self._segs)
+        b = sorted(other._segs)
+        i = j = 0
+        while i < len(a) and j < len(b):
+            lo = max(a[i][0], b[j][0])
+            hi = min(a[i][1], b[j][1])
+            if hi > lo:
+                out._segs.append([lo, hi])
+            if a[i][1] < b[j][1]:
+                i += 1
+            else:
+                j += 1
+        return out
+
+    def __getitem__(self, index):
+        if not isinstance(index, slice):
+            raise IndexError("RangesInt32 supports slice indexing only")
+        start, stop, step = index.indices(self.count)
+        if step != 1:
+            raise IndexError("RangesInt32 slices must have unit step")
+        out = RangesInt32(max(0, stop - start), self.reference + start)
+        for a, b in self._segs:
+            lo, hi = max(a, start) - start, min(b, stop) - start
+            if hi > lo:
+                out._segs.append([lo, hi])
+        return out
+
+    def __repr__(self):
+        return "RangesInt32(n=%d:rngs=%d)" % (self.count, len(self._segs))
+
+
+class RangesMatrix:
+    """A grid of RangesInt32 objects (python/proj/ranges.py:11-297)."""
+
+    def __init__(self, items=(), child_shape=None, skip_shape_check=False):
+        self.ranges = [x for x in items]
+        if len(self.ranges):
+            child_shape = self.ranges[0].shape
+            if not skip_shape_check:
+                assert all(item.shape == child_shape for item in self.ranges)
+        elif child_shape is None:
+            child_shape = ()
+        self._child_shape = tuple(child_shape)
+
+    @property
+    def shape(self):
+        if not self.ranges:
+            return (0,) + self._child_shape
+        return (len(self.ranges),) + tuple(self.ranges[0].shape)
+
+    def __len__(self):
+        return self.shape[0]
+
+    def __iter__(self):
+        return iter(self.ranges)
+
+    def __repr__(self):
+        return "RangesMatrix(" + ",".join(map(str, self.shape)) + ")"
+
+    def copy(self):
+        return RangesMatrix([x.copy() for x in self.ranges], child_shape=self.shape[1:])
+
+    def zeros_like(self):
+        return RangesMatrix([x.zeros_like() for x in self.ranges], child_shape=self.shape[1:])
+
+    def ones_like(self):
+        return RangesMatrix([x.ones_like() for x in self.ranges], child_shape=self.shape[1:])
+
+    def mask(self, dest=None):
+        if not self.ranges:
+            out = np.zeros(self.shape, dtype=bool)
+        else:
+            out = np.array([r.mask() for r in self.ranges])
+        if dest is not None:
+            dest[...] = out
+            return dest
+        return out
+
+    def __getitem__(self, index):
+        if isinstance(index, tuple):
+            if len(index) == 0:
+                return self
+            head, rest = index[0], index[1:]
+        else:
+            head, rest = index, ()
+        if isinstance(head, (int, np.integer)):
+            item = self.ranges[int(head)]
+            return item[rest] if rest else item
+        if isinstance(head, slice):
+            items = self.ranges[head]
+        else:
+            sel = np.arange(len(self.ranges))[head]
+            items = [self.ranges[i] for i in np.atleast_1d(sel)]
+        if rest:
+            items = [x[rest if len(rest) > 1 else rest[0]] for x in items]
+        return RangesMatrix(items, child_shape=self.shape[1:])
+
+    def __invert__(self):
+        return RangesMatrix([~x for x in self.ranges], child_shape=self.shape[1:])
+
+    def __mul__(self, other):
+        if isinstance(other, RangesMatrix) and len(other.shape) == len(self.shape):
+            return RangesMatrix([a * b for a, b in zip(self.ranges, other.ranges)],
+                                child_shape=self.shape[1:])
+        return RangesMatrix([a * other for a in self.ranges], child_shape=self.shape[1:])
+
+    def __add__(self, other):
+        if isinstance(other, RangesMatrix) and len(other.shape) == len(self.shape):
+            return RangesMatrix([a + b for a, b in zip(self.ranges, other.ranges)],
+                                child_shape=self.shape[1:])
+        return RangesMatrix([a + other for a in self.ranges], child_shape=self.shape[1:])
+
+    @classmethod
+    def zeros(cls, shape):
+        shape = tuple(shape)
+        if len(shape) == 1:
+            return RangesInt32(shape[0])
+        return cls([cls.zeros(shape[1:]) for _ in range(shape[0])], child_shape=shape[1:])
+
+    @classmethod
+    def ones(cls, shape):
+        shape = tuple(shape)
+        if len(shape) == 1:
+            return RangesInt32(shape[0]).ones_like()
+        return cls([cls.ones(shape[1:]) for _ in range(shape[0])], child_shape=shape[1:])
+
+    @classmethod
+    def from_mask(cls, mask):
+        mask = np.asarray(mask, dtype=bool)
+        if mask.ndim == 1:
+            return RangesInt32.from_mask(mask)
+        return cls([cls.from_mask(m) for m in mask], child_shape=mask.shape[1:])
+
+
+def wrap_ivals(ivals):
+    """Nested lists of RangesInt32 [bunch][thread][det] -> list of
+    RangesMatrix (python/proj/wcs.py:887-915)."""
+    return [RangesMatrix([RangesMatrix(y) for y in x]) for x in ivals]
