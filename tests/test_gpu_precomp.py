@@ -52,8 +52,10 @@ def test_precomp_matches_on_the_fly(orc, gpulib, tiled, ncomp):
     s2 = np.array(c.eng.from_map(src, c.bore, c.dets, c.resp, None))
     # Precomp sums the components in float32 before adding (:2073-2080),
     # on-the-fly adds each term to the float32 signal: equal to float32
-    # rounding.
-    np.testing.assert_allclose(s1, s2, rtol=1e-5, atol=1e-5)
+    # rounding, on the samples pointing_matrix puts on the map.
+    on = pix[..., 0] >= 0
+    np.testing.assert_allclose(s1[on], s2[on], rtol=1e-5, atol=1e-5)
+    assert np.all(s1[~on] == 0)
 
 
 @pytest.mark.parametrize("tiled", [False, True])
