@@ -93,6 +93,10 @@ _SIGS = {
     "so3g_proj_to_map": (ctypes.c_int, [P(Pixelization), c_void_p, c_int32, c_void_p, c_int32,
                                         c_void_p, c_void_p, c_int64, c_void_p, P(Ranges),
                                         P(Map), c_int32, c_void_p, c_void_p]),
+    "so3g_proj_to_map_noalloc": (ctypes.c_int, [P(Pixelization), c_void_p, c_int32, c_void_p,
+                                                c_int32, c_void_p, c_void_p, c_int64, c_void_p,
+                                                c_void_p, c_int32, c_void_p, c_void_p, c_int32,
+                                                c_int32, c_void_p, c_void_p]),
     "so3g_proj_to_weight_map": (ctypes.c_int, [P(Pixelization), c_void_p, c_int32, c_void_p,
                                                c_int32, c_void_p, c_void_p, P(Ranges), P(Map),
                                                c_int32, c_void_p, c_void_p]),

@@ -21,17 +21,18 @@ std::atomic<long long> g_launches{0};
 std::mutex g_mu;
 constexpr int kMaxDevices = 64;
 double *g_lut[kMaxDevices] = {nullptr};
-std::vector<double> g_host_lut;
+double g_host_lut[2 * kLutN];
+bool g_host_lut_ready = false;
 
 // asinTable / atan2Table construction (include/so_linterp.h:35-39, 51-56),
 // with the host math library, as the reference's static tables
 // (src/Projection.cxx:36-38).
 void build_host_tables() {
-    if (!g_host_lut.empty()) return;
-    g_host_lut.resize(2 * kLutN);
+    if (g_host_lut_ready) return;
     const double dx = 1. / (kLutN - 1);
     for (int i = 0; i < kLutN; i++) g_host_lut[i] = std::asin(i * dx);
     for (int i = 0; i < kLutN; i++) g_host_lut[kLutN + i] = std::atan2(i * dx, 1.);
+    g_host_lut_ready = true;
 }
 
 bool pow2(long long v) { return v > 0 && (v & (v - 1)) == 0; }
@@ -69,7 +70,19 @@ int pix_kind(const so3g_pixelization *pz) {
     return (pz->tiled ? 2 : 0) + (pz->interp == SO3G_INTERP_BILINEAR ? 1 : 0);
 }
 
+const double *host_lut() {
+    std::lock_guard<std::mutex> lk(g_mu);
+    build_host_tables();
+    return g_host_lut;
+}
+
 int make_geom(const so3g_pixelization *pz, DGeom *g) {
+    const double *lut = device_lut();
+    if (!lut) return set_error(SO3G_ERR_NOT_INIT, "so3g_init() was not called on this device");
+    return make_geom_lut(pz, g, lut);
+}
+
+int make_geom_lut(const so3g_pixelization *pz, DGeom *g, const double *lut) {
     if (!pz) return set_error(SO3G_ERR_ARGUMENT, "pixelization is NULL");
     std::memset(g, 0, sizeof(*g));
     if (pz->n_comp < 1 || pz->n_comp > 3)
@@ -79,8 +92,7 @@ int make_geom(const so3g_pixelization *pz, DGeom *g) {
     if (pz->interp != SO3G_INTERP_NEAREST && pz->interp != SO3G_INTERP_BILINEAR)
         return set_error(SO3G_ERR_ARGUMENT, "unknown interpolation %d", pz->interp);
     g->ncomp = pz->n_comp;
-    g->lut = device_lut();
-    if (!g->lut) return set_error(SO3G_ERR_NOT_INIT, "so3g_init() was not called on this device");
+    g->lut = lut;
     if (pz->pix_sys == SO3G_PIX_HEALPIX) {
         if (pz->coord_sys != SO3G_COORD_CAR)
             return set_error(SO3G_ERR_ARGUMENT, "HEALPix pixelization needs CAR coordinates");
@@ -165,7 +177,7 @@ int so3g_init(void) {
     double *d = nullptr;
     e = cudaMalloc(&d, sizeof(double) * 2 * kLutN);
     if (e != cudaSuccess) return set_error(SO3G_ERR_CUDA, "cudaMalloc: %s", cudaGetErrorString(e));
-    e = cudaMemcpy(d, g_host_lut.data(), sizeof(double) * 2 * kLutN, cudaMemcpyHostToDevice);
+    e = cudaMemcpy(d, g_host_lut, sizeof(double) * 2 * kLutN, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         cudaFree(d);
         return set_error(SO3G_ERR_CUDA, "cudaMemcpy: %s", cudaGetErrorString(e));
@@ -181,8 +193,8 @@ int so3g_get_trig_tables(double *asin_vals, double *atan2_vals, int32_t n) {
         std::lock_guard<std::mutex> lk(g_mu);
         build_host_tables();
     }
-    std::memcpy(asin_vals, g_host_lut.data(), sizeof(double) * kLutN);
-    std::memcpy(atan2_vals, g_host_lut.data() + kLutN, sizeof(double) * kLutN);
+    std::memcpy(asin_vals, g_host_lut, sizeof(double) * kLutN);
+    std::memcpy(atan2_vals, g_host_lut + kLutN, sizeof(double) * kLutN);
     return SO3G_OK;
 }
 

@@ -17,8 +17,13 @@ int after_launch(const char *what);
 // Per-device trig table (asin then atan2, 2 x kLutN float64), or NULL.
 const double *device_lut();
 
-// Validates a pixelization and fills the device geometry (without the map).
+// Validates a pixelization and fills the device geometry (without the map),
+// using the trig tables uploaded by so3g_init().
 int make_geom(const so3g_pixelization *pz, DGeom *g);
+// The same with the caller's device copy of the trig tables.
+int make_geom_lut(const so3g_pixelization *pz, DGeom *g, const double *lut);
+// The host trig tables (asin then atan2, 2 x kLutN float64).
+const double *host_lut();
 // Adds the map's tile table to the geometry; checks the tile count.
 int attach_map(const so3g_pixelization *pz, const so3g_map *m, DGeom *g);
 // Pixelizor kind (PX_*) of a pixelization.
