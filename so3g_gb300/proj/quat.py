@@ -107,7 +107,7 @@ class G3VectorQuat(np.ndarray):
         return np.asarray(r)
 
     def __setitem__(self, idx, value):
-        np.ndarray.__setitem__(self, idx, np.asarray(value))
+        self.view(np.ndarray)[idx] = np.asarray(value)
 
     def __mul__(self, other):
         if isinstance(other, quat):
@@ -123,7 +123,7 @@ class G3VectorQuat(np.ndarray):
 
     def __imul__(self, other):
         res = self * other
-        np.ndarray.__setitem__(self, Ellipsis, np.asarray(res))
+        self.view(np.ndarray)[...] = np.asarray(res)
         return self
 
     def __invert__(self):
