@@ -221,7 +221,8 @@ def run_ours(args, c, rank, world):
             t["from_map"] = (e0, e1)
         return t
 
-    def timed(accum, steps, warmup):
+    def timed(accum, steps, warmup, pointing=_abi.POINTING_CERTIFIED):
+        eng.pointing = pointing
         for _ in range(warmup):
             step(accum)
         torch.cuda.synchronize()
@@ -253,7 +254,11 @@ def run_ours(args, c, rank, world):
         ms = float(t.item())
     res = {"ms_per_step": ms, "op_ms": op_ms, "launches": launches, "clocks": clocks}
     if not args.no_fp64_path and world == 1:
-        ms64, op64, _, _ = timed(_abi.ACCUM_ATOMIC, max(1, args.steps // 2), 1)
+        # The plain float64 GPU path: exact float64 pointing, one float64
+        # atomic per term.
+        ms64, op64, _, _ = timed(_abi.ACCUM_ATOMIC, max(1, args.steps // 2), 1,
+                                 pointing=_abi.POINTING_EXACT)
+        eng.pointing = _abi.POINTING_CERTIFIED
         res["fp64_path"] = {"ms_per_step": ms64, "op_ms": op64}
     # to_weight_map, timed on its own (not part of the step).
     if world == 1:
@@ -410,7 +415,8 @@ def main():
     cfg = {"workload": workload, "n_det": c["n_det"], "n_time": c["n_time"],
            "map": [3] + list(c["shape"]), "step": args.ops.replace(",", " + "),
            "l2": "inputs larger than L2 (TOD %.1f GB)" % (c["n_det"] * c["n_time"] * 4 / 1e9),
-           "precision": "float64 pointing, float32 products, float64 map accumulation",
+           "precision": "pointing certified equal to float64 (double-float with float64 "
+                        "fallback), float32 products, float64 map accumulation",
            "parallelism": "replicas" if world > 1 else "single GPU"}
 
     if args.impl == "reference":

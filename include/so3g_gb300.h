@@ -45,7 +45,7 @@
 extern "C" {
 #endif
 
-#define SO3G_GB300_ABI_VERSION 1
+#define SO3G_GB300_ABI_VERSION 2
 
 /* Coordinate systems: the CoordSys template parameter (Pointer<C>),
  * src/Projection.cxx:152-159, 238-507. */
@@ -84,6 +84,18 @@ enum so3g_accum {
     SO3G_ACCUM_WARP_RUNS = 1
 };
 
+/* Pointing evaluation (so3g_pixelization.pointing). */
+enum so3g_pointing {
+    /* Float64 throughout, in the reference's operation order. */
+    SO3G_POINTING_EXACT = 0,
+    /* CAR with nearest-neighbour flat pixelizors: double-float pointing
+     * whose pixel indices and float32 spin factors are certified equal to
+     * the exact ones, with the exact path for every sample that cannot be
+     * certified -- the results are those of SO3G_POINTING_EXACT.  Other
+     * pixelizations use the exact path. */
+    SO3G_POINTING_CERTIFIED = 1
+};
+
 /* Status codes returned by every entry point. */
 enum so3g_status {
     SO3G_OK            = 0,
@@ -120,6 +132,7 @@ typedef struct so3g_pixelization {
     int32_t nside;          /* HEALPix nside */
     int32_t nest;           /* HEALPix: 1 = NEST, 0 = RING */
     int32_t nside_tile;     /* HEALPix Tiled */
+    int32_t pointing;       /* enum so3g_pointing */
     double  cdelt[2];       /* Flat: (dy, dx), radians per pixel */
     double  crpix[2];       /* Flat: (crpix_y, crpix_x), FITS 1-based */
 } so3g_pixelization;

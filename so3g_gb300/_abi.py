@@ -18,7 +18,8 @@ PIX_FLAT, PIX_HEALPIX = 0, 1
 INTERP_NEAREST, INTERP_BILINEAR = 0, 1
 ACCUM_ATOMIC, ACCUM_WARP_RUNS = 0, 1
 DEVERR_NONE, DEVERR_MISSING_TILE, DEVERR_PIXEL_RANGE = 0, 1, 2
-ABI_VERSION = 1
+ABI_VERSION = 2
+POINTING_EXACT, POINTING_CERTIFIED = 0, 1
 LUT_N = 1 << 14
 
 c_int32 = ctypes.c_int32
@@ -39,6 +40,7 @@ class Pixelization(ctypes.Structure):
         ("nside", c_int32),
         ("nest", c_int32),
         ("nside_tile", c_int32),
+        ("pointing", c_int32),
         ("cdelt", c_double * 2),
         ("crpix", c_double * 2),
     ]

@@ -21,8 +21,25 @@ std::atomic<long long> g_launches{0};
 std::mutex g_mu;
 constexpr int kMaxDevices = 64;
 double *g_lut[kMaxDevices] = {nullptr};
+float4 *g_fast_lut[kMaxDevices] = {nullptr};
 double g_host_lut[2 * kLutN];
 bool g_host_lut_ready = false;
+
+// Double-float knots of a table and their forward differences, for the
+// certified pointing: (v_hi, v_lo, dv_hi, dv_lo) per knot.
+void split(double x, float &hi, float &lo) {
+    hi = (float)x;
+    lo = (float)(x - (double)hi);
+}
+
+void fast_knots(const double *v, float4 *out) {
+    for (int i = 0; i < kLutN; i++) {
+        float vh, vl, dh, dl;
+        split(v[i], vh, vl);
+        split(i + 1 < kLutN ? v[i + 1] - v[i] : 0., dh, dl);
+        out[i] = make_float4(vh, vl, dh, dl);
+    }
+}
 
 // asinTable / atan2Table construction (include/so_linterp.h:35-39, 51-56),
 // with the host math library, as the reference's static tables
@@ -63,6 +80,29 @@ const double *device_lut() {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
     return g_lut[dev];
+}
+
+FastTables device_fast_tables() {
+    int dev = 0;
+    FastTables t{nullptr, nullptr};
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return t;
+    if (g_fast_lut[dev]) {
+        t.asin_t = g_fast_lut[dev];
+        t.atan2_t = g_fast_lut[dev] + kLutN;
+    }
+    return t;
+}
+
+FastConst make_fast_const(const DGeom &g) {
+    FastConst c;
+    const double inv_x = g.cdx != 0. ? 1. / g.cdx : 0., inv_y = g.cdy != 0. ? 1. / g.cdy : 0.;
+    split(inv_x, c.inv_cdx.hi, c.inv_cdx.lo);
+    split(inv_y, c.inv_cdy.hi, c.inv_cdy.lo);
+    split(g.crx - 1 + 0.5, c.off_x.hi, c.off_x.lo);
+    split(g.cry - 1 + 0.5, c.off_y.hi, c.off_y.lo);
+    split(kPi, c.pi.hi, c.pi.lo);
+    split(kPi / 2, c.half_pi.hi, c.half_pi.lo);
+    return c;
 }
 
 int pix_kind(const so3g_pixelization *pz) {
@@ -183,6 +223,19 @@ int so3g_init(void) {
         return set_error(SO3G_ERR_CUDA, "cudaMemcpy: %s", cudaGetErrorString(e));
     }
     g_lut[dev] = d;
+    // Double-float knots for the certified pointing.
+    static float4 knots[2 * kLutN];
+    fast_knots(g_host_lut, knots);
+    fast_knots(g_host_lut + kLutN, knots + kLutN);
+    float4 *f = nullptr;
+    e = cudaMalloc(&f, sizeof(float4) * 2 * kLutN);
+    if (e != cudaSuccess) return set_error(SO3G_ERR_CUDA, "cudaMalloc: %s", cudaGetErrorString(e));
+    e = cudaMemcpy(f, knots, sizeof(float4) * 2 * kLutN, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(f);
+        return set_error(SO3G_ERR_CUDA, "cudaMemcpy: %s", cudaGetErrorString(e));
+    }
+    g_fast_lut[dev] = f;
     return SO3G_OK;
 }
 

@@ -1,12 +1,19 @@
-// gather.cu -- from_map: per-sample float64 pointing and a gather from the
-// map, accumulated into the float32 signal exactly as the reference does
-// (each term added in float64 and rounded to float32).
+// gather.cu -- from_map: per-sample pointing and a gather from the map,
+// accumulated into the float32 signal exactly as the reference does (each
+// term added in float64 and rounded to float32).
+//
+// CAR with a nearest-neighbour flat pixelizor uses the certified
+// double-float pointing of fastpoint.cuh (when GatherArgs::fast is set);
+// samples it cannot certify are queued in shared memory and finished by the
+// exact float64 pointing, so every sample's result equals the exact path's.
 
 #include "host.h"
 
 namespace so3g {
 
 namespace {
+
+constexpr int kQueueCap = 512;
 
 struct GatherArgs {
     DGeom g;
@@ -19,42 +26,96 @@ struct GatherArgs {
     Segs segs;
     int piece;
     int *err;
+    int fast;
+    FastTables ft;
+    FastConst fc;
 };
+
+// Adds the sample's map terms to its signal (src/Projection.cxx:1763-1765).
+template <int P, int NT>
+__device__ __forceinline__ void gather_taps(const GatherArgs &a, float *sp, int n,
+                                            const int (*pix)[3], const float *w,
+                                            const float *pf) {
+    float sig = *sp;
+    const int nc = a.g.ncomp;
+#pragma unroll
+    for (int k = 0; k < NT; k++) {
+        if (k >= n) break;
+        long long off, plane;
+        int bad = locate<P>(a.g, pix[k], &off, &plane);
+        if (bad >= 0) {
+            record_missing_tile(a.err, bad);
+            continue;
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+            if (c < nc) sig += __ldg(a.map + off + c * plane) * pf[c] * w[k];
+    }
+    *sp = sig;
+}
+
+template <int C, int P>
+__device__ void exact_gather(const GatherArgs &a, int det, int t, const QuatD &ofs, float T,
+                             float Pr) {
+    constexpr int NT = PixTraits<P>::taps;
+    double coords[4];
+    float pf[3];
+    int pix[NT][3];
+    float w[NT];
+    get_coords<C>(a.g.lut, load_quat(a.bore + 4LL * t), ofs, coords);
+    spin_factors(a.g.ncomp, coords, T, Pr, pf);
+    const int n = get_pixels<P>(a.g, coords, pix, w);
+    gather_taps<P, NT>(a, a.signal + det * a.sig_stride + t, n, pix, w, pf);
+}
 
 template <int C, int P>
 __global__ void __launch_bounds__(kBlock) k_from_map(GatherArgs a) {
+    constexpr bool kFastOK =
+        C == SO3G_COORD_CAR && (P == PX_FLAT_NT_NN || P == PX_FLAT_T_NN);
+    __shared__ int s_queue[kFastOK ? kQueueCap : 1];
+    __shared__ int s_qn;
     int det, t0, t1;
     if (!seg_piece(a.segs, a.piece, det, t0, t1)) return;
     const QuatD ofs = load_quat(a.dets + 4LL * det);
     const float T = __ldg(a.resp + 2 * det), Pr = __ldg(a.resp + 2 * det + 1);
     const int nc = a.g.ncomp;
     constexpr int NT = PixTraits<P>::taps;
-    for (int t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
-        double coords[4];
-        float pf[3];
-        int pix[NT][3];
-        float w[NT];
-        const QuatD qb = load_quat(a.bore + 4LL * t);
-        get_coords<C>(a.g.lut, qb, ofs, coords);
-        spin_factors(nc, coords, T, Pr, pf);
-        float *sp = a.signal + det * a.sig_stride + t;
-        float sig = *sp;
-        int n = get_pixels<P>(a.g, coords, pix, w);
-#pragma unroll
-        for (int k = 0; k < NT; k++) {
-            if (k >= n) break;
-            long long off, plane;
-            int bad = locate<P>(a.g, pix[k], &off, &plane);
-            if (bad >= 0) {
-                record_missing_tile(a.err, bad);
-                continue;
+    if (!(kFastOK && a.fast)) {
+        for (int t = t0 + threadIdx.x; t < t1; t += blockDim.x) exact_gather<C, P>(a, det, t, ofs, T, Pr);
+        return;
+    }
+    dfl qd[4] = {df_from_double(ofs.a), df_from_double(ofs.b), df_from_double(ofs.c),
+                 df_from_double(ofs.d)};
+    if (threadIdx.x == 0) s_qn = 0;
+    __syncthreads();
+    const int rounds = (t1 - t0 + blockDim.x - 1) / blockDim.x;
+    for (int r = 0; r < rounds; r++) {
+        const int t = t0 + r * blockDim.x + threadIdx.x;
+        if (t < t1) {
+            const double *bp = a.bore + 4LL * t;
+            const double2 lo = __ldg(reinterpret_cast<const double2 *>(bp));
+            const double2 hi = __ldg(reinterpret_cast<const double2 *>(bp) + 1);
+            const dfl qb[4] = {df_from_double(lo.x), df_from_double(lo.y), df_from_double(hi.x),
+                               df_from_double(hi.y)};
+            int pix[NT][3];
+            float w[NT] = {1.f};
+            float pf[3];
+            bool on = false;
+            if (fast_car<P>(a.g, a.ft, a.fc, qb, qd, nc, T, Pr, pix[0], &on, pf)) {
+                if (on) gather_taps<P, NT>(a, a.signal + det * a.sig_stride + t, 1, pix, w, pf);
+            } else {
+                s_queue[atomicAdd(&s_qn, 1)] = t;
             }
-            // src/Projection.cxx:1763-1765
-#pragma unroll
-            for (int c = 0; c < 3; c++)
-                if (c < nc) sig += __ldg(a.map + off + c * plane) * pf[c] * w[k];
         }
-        *sp = sig;
+        __syncthreads();
+        const int qn = s_qn;
+        if (qn > kQueueCap - (int)blockDim.x || r == rounds - 1) {
+            for (int i = threadIdx.x; i < qn; i += blockDim.x)
+                exact_gather<C, P>(a, det, s_queue[i], ofs, T, Pr);
+            __syncthreads();
+            if (threadIdx.x == 0) s_qn = 0;
+            __syncthreads();
+        }
     }
 }
 
@@ -97,6 +158,9 @@ extern "C" int so3g_proj_from_map(const so3g_pixelization *pz, const double *bor
     L.a.segs = Segs{nullptr, n_time};
     L.a.piece = piece_len(n_time);
     L.a.err = err;
+    L.a.ft = device_fast_tables();
+    L.a.fc = make_fast_const(L.a.g);
+    L.a.fast = (pz->pointing == SO3G_POINTING_CERTIFIED && L.a.ft.asin_t) ? 1 : 0;
     L.grid = dim3((unsigned)n_det, (unsigned)((n_time + L.a.piece - 1) / L.a.piece));
     L.stream = (cudaStream_t)stream;
     return dispatch_cp(pz->coord_sys, pix_kind(pz), L);

@@ -4,7 +4,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 #include "../../include/so3g_gb300.h"
-#include "device.cuh"
+#include "fastpoint.cuh"
 
 namespace so3g {
 
@@ -24,6 +24,11 @@ int make_geom(const so3g_pixelization *pz, DGeom *g);
 int make_geom_lut(const so3g_pixelization *pz, DGeom *g, const double *lut);
 // The host trig tables (asin then atan2, 2 x kLutN float64).
 const double *host_lut();
+// Double-float knot tables of the certified pointing on the current device
+// (uploaded by so3g_init), or NULL pointers.
+FastTables device_fast_tables();
+// Double-float pixelizor constants of the certified pointing.
+FastConst make_fast_const(const DGeom &g);
 // Adds the map's tile table to the geometry; checks the tile count.
 int attach_map(const so3g_pixelization *pz, const so3g_map *m, DGeom *g);
 // Pixelizor kind (PX_*) of a pixelization.

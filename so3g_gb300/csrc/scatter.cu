@@ -52,6 +52,9 @@ int scatter_entry(const so3g_pixelization *pz, const double *bore, int32_t n_tim
     L.a.accum = accum;
     L.a.err = err;
     L.a.map = map->data;
+    L.a.ft = device_fast_tables();
+    L.a.fc = make_fast_const(L.a.g);
+    L.a.fast = (pz->pointing == SO3G_POINTING_CERTIFIED && L.a.ft.asin_t) ? 1 : 0;
     L.grid = dim3((unsigned)n_seg, (unsigned)((max_len + L.a.piece - 1) / L.a.piece));
     L.stream = (cudaStream_t)stream;
     return dispatch_cp(pz->coord_sys, pix_kind(pz), L);

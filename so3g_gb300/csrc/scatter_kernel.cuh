@@ -2,21 +2,30 @@
 // entry points of scatter.cu and noalloc.cu.
 //
 // Work layout: block (x, y) takes piece y of sample segment x (one detector
-// and a contiguous range of its samples); each warp handles 32 consecutive
-// samples at a time, lane = sample.  Consecutive samples of a scanning
+// and a contiguous range of its samples) in rounds of blockDim.x
+// consecutive samples, lane = sample.  Consecutive samples of a scanning
 // detector tend to fall in the same pixel, which the WARP_RUNS accumulator
 // exploits: runs of equal pixels across the warp are summed in registers
 // (compensated float32) and flushed with one float64 atomic per run and
 // component.  The ATOMIC accumulator adds every term on its own.
+//
+// Pointing: CAR with a nearest-neighbour flat pixelizor uses the certified
+// double-float pointing of fastpoint.cuh when ScatterArgs::fast is set;
+// samples it cannot certify are queued in shared memory and recomputed by
+// the exact float64 pointing, with plain atomics, when the queue fills and
+// at the end of the piece.  Every other case uses the exact pointing.
 #pragma once
 
 #include "host.h"
+#include "fastpoint.cuh"
 
 namespace so3g {
 
 // Internal linkage: every translation unit that includes this header gets
 // its own instantiations.
 namespace {
+
+constexpr int kQueueCap = 512;
 
 struct ScatterArgs {
     DGeom g;
@@ -31,26 +40,21 @@ struct ScatterArgs {
     int accum;
     int *err;
     double *map;
+    int fast;
+    FastTables ft;
+    FastConst fc;
 };
 
-template <int C, int P, bool WEIGHT>
-__global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs a) {
-    int det, t0, t1;
-    if (!seg_piece(a.segs, a.piece, det, t0, t1)) return;
-    float det_wt = 1.f;
-    if (a.det_weights) {
-        det_wt = __ldg(a.det_weights + det);
-        if (det_wt == 0.f) return;  // src/Projection.cxx:1784-1788
-    }
-    const QuatD ofs = load_quat(a.dets + 4LL * det);
-    const float T = __ldg(a.resp + 2 * det), Pr = __ldg(a.resp + 2 * det + 1);
-    const int nc = a.g.ncomp;
-    const int lane = threadIdx.x & 31;
-    constexpr int NT = PixTraits<P>::taps;
-    constexpr int NV = WEIGHT ? 6 : 3;
-    // Value slots: to_map slot c = component c; to_weight_map slots are the
-    // upper-triangle pairs (i, j), j >= i, in row order.
-    int mult[NV];
+template <int C, int P>
+struct FastEligible {
+    static constexpr bool value =
+        C == SO3G_COORD_CAR && (P == PX_FLAT_NT_NN || P == PX_FLAT_T_NN);
+};
+
+// Value slots: to_map slot c = component c; to_weight_map slots are the
+// upper-triangle pairs (i, j), j >= i, in row order.
+template <bool WEIGHT>
+__device__ __forceinline__ unsigned value_slots(int nc, int *mult) {
     unsigned vmask = 0;
     if (!WEIGHT) {
 #pragma unroll
@@ -68,22 +72,118 @@ __global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs a) {
                 if (i < nc && j < nc) vmask |= 1u << k;
             }
     }
+    return vmask;
+}
 
-    for (int base = t0 + (threadIdx.x & ~31); base < t1; base += blockDim.x) {
-        const int t = base + lane;
+template <bool WEIGHT, int NV>
+__device__ __forceinline__ void tap_values(float sig, const float *pf, float w, float det_wt,
+                                           float (&v)[NV]) {
+    if (!WEIGHT) {
+        // src/Projection.cxx:1807 -- float32 product, left to right
+#pragma unroll
+        for (int c = 0; c < 3; c++) v[c] = sig * pf[c] * w * det_wt;
+    } else {
+        // src/Projection.cxx:1850
+        int s = 0;
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = i; j < 3; j++, s++) v[s] = pf[i] * pf[j] * w * w * det_wt;
+    }
+}
+
+// One sample through the exact float64 pointing, added with plain atomics.
+template <int C, int P, bool WEIGHT>
+__device__ void exact_sample(const ScatterArgs &a, int det, int t, const QuatD &ofs, float T,
+                             float Pr, float det_wt, const int *mult, unsigned vmask) {
+    constexpr int NT = PixTraits<P>::taps;
+    constexpr int NV = WEIGHT ? 6 : 3;
+    double coords[4];
+    float pf[3];
+    int pix[NT][3];
+    float w[NT];
+    get_coords<C>(a.g.lut, load_quat(a.bore + 4LL * t), ofs, coords);
+    spin_factors(a.g.ncomp, coords, T, Pr, pf);
+    const float sig = WEIGHT ? 0.f : __ldg(a.signal + det * a.sig_stride + t);
+    const int n = get_pixels<P>(a.g, coords, pix, w);
+    for (int k = 0; k < n; k++) {
+        long long off, plane;
+        int bad = locate<P>(a.g, pix[k], &off, &plane);
+        if (bad >= 0) {
+            record_missing_tile(a.err, bad);
+            continue;
+        }
+        float v[NV];
+        tap_values<WEIGHT>(sig, pf, w[k], det_wt, v);
+#pragma unroll
+        for (int s = 0; s < NV; s++)
+            if ((vmask >> s) & 1u) atomicAdd(a.map + off + mult[s] * plane, (double)v[s]);
+    }
+}
+
+template <int C, int P, bool WEIGHT>
+__global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs a) {
+    constexpr bool kFastOK = FastEligible<C, P>::value;
+    __shared__ int s_queue[kFastOK ? kQueueCap : 1];
+    __shared__ int s_qn;
+    int det, t0, t1;
+    if (!seg_piece(a.segs, a.piece, det, t0, t1)) return;
+    float det_wt = 1.f;
+    if (a.det_weights) {
+        det_wt = __ldg(a.det_weights + det);
+        if (det_wt == 0.f) return;  // src/Projection.cxx:1784-1788
+    }
+    const QuatD ofs = load_quat(a.dets + 4LL * det);
+    const float T = __ldg(a.resp + 2 * det), Pr = __ldg(a.resp + 2 * det + 1);
+    const int nc = a.g.ncomp;
+    constexpr int NT = PixTraits<P>::taps;
+    constexpr int NV = WEIGHT ? 6 : 3;
+    int mult[NV];
+    const unsigned vmask = value_slots<WEIGHT>(nc, mult);
+    const bool fast = kFastOK && a.fast;
+    dfl qd[4];
+    if (kFastOK && fast) {
+        qd[0] = df_from_double(ofs.a);
+        qd[1] = df_from_double(ofs.b);
+        qd[2] = df_from_double(ofs.c);
+        qd[3] = df_from_double(ofs.d);
+        if (threadIdx.x == 0) s_qn = 0;
+        __syncthreads();
+    }
+    const int rounds = (t1 - t0 + blockDim.x - 1) / blockDim.x;
+    for (int r = 0; r < rounds; r++) {
+        const int t = t0 + r * blockDim.x + threadIdx.x;
         const bool live = t < t1;
-        double coords[4];
         float pf[3] = {0.f, 0.f, 0.f};
         int pix[NT][3];
         float w[NT];
         int n = 0;
         float sig = 0.f;
         if (live) {
-            const QuatD qb = load_quat(a.bore + 4LL * t);
-            get_coords<C>(a.g.lut, qb, ofs, coords);
-            spin_factors(nc, coords, T, Pr, pf);
-            if (!WEIGHT) sig = __ldg(a.signal + det * a.sig_stride + t);
-            n = get_pixels<P>(a.g, coords, pix, w);
+            bool done = false;
+            if (kFastOK && fast) {
+                const double *bp = a.bore + 4LL * t;
+                const double2 lo = __ldg(reinterpret_cast<const double2 *>(bp));
+                const double2 hi = __ldg(reinterpret_cast<const double2 *>(bp) + 1);
+                const dfl qb[4] = {df_from_double(lo.x), df_from_double(lo.y),
+                                   df_from_double(hi.x), df_from_double(hi.y)};
+                bool on = false;
+                if (fast_car<P>(a.g, a.ft, a.fc, qb, qd, nc, T, Pr, pix[0], &on, pf)) {
+                    n = on ? 1 : 0;
+                    w[0] = 1.f;
+                } else {
+                    s_queue[atomicAdd(&s_qn, 1)] = t;
+                    n = 0;
+                }
+                done = true;
+            }
+            if (!done) {
+                double coords[4];
+                get_coords<C>(a.g.lut, load_quat(a.bore + 4LL * t), ofs, coords);
+                spin_factors(nc, coords, T, Pr, pf);
+                n = get_pixels<P>(a.g, coords, pix, w);
+            }
+            if (!WEIGHT && n > 0) sig = __ldg(a.signal + det * a.sig_stride + t);
         }
 #pragma unroll
         for (int k = 0; k < NT; k++) {
@@ -96,17 +196,8 @@ __global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs a) {
                 if (bad >= 0) {
                     record_missing_tile(a.err, bad);
                     off = -1;
-                } else if (!WEIGHT) {
-                    // src/Projection.cxx:1807 -- float32 product, left to right
-#pragma unroll
-                    for (int c = 0; c < 3; c++) v[c] = sig * pf[c] * w[k] * det_wt;
                 } else {
-                    // src/Projection.cxx:1850
-                    int s = 0;
-#pragma unroll
-                    for (int i = 0; i < 3; i++)
-#pragma unroll
-                        for (int j = i; j < 3; j++, s++) v[s] = pf[i] * pf[j] * w[k] * w[k] * det_wt;
+                    tap_values<WEIGHT>(sig, pf, w[k], det_wt, v);
                 }
             }
             if (NT > 1 && !__any_sync(kFull, off >= 0)) continue;
@@ -116,6 +207,18 @@ __global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs a) {
 #pragma unroll
                 for (int s = 0; s < NV; s++)
                     if ((vmask >> s) & 1u) atomicAdd(a.map + off + mult[s] * plane, (double)v[s]);
+            }
+        }
+        if (kFastOK && fast) {
+            __syncthreads();
+            const int qn = s_qn;
+            if (qn > kQueueCap - (int)blockDim.x || r == rounds - 1) {
+                for (int i = threadIdx.x; i < qn; i += blockDim.x)
+                    exact_sample<C, P, WEIGHT>(a, det, s_queue[i], ofs, T, Pr, det_wt, mult,
+                                               vmask);
+                __syncthreads();
+                if (threadIdx.x == 0) s_qn = 0;
+                __syncthreads();
             }
         }
     }

@@ -28,6 +28,10 @@ INT32_MAX = 2**31 - 1
 
 # Default scatter accumulator: warp pre-reduction of pixel runs.
 DEFAULT_ACCUM = _abi.ACCUM_WARP_RUNS
+# Default pointing evaluation: certified double-float where available (its
+# results equal the exact float64 path's); set an engine's ``pointing``
+# attribute to _abi.POINTING_EXACT to force float64 everywhere.
+DEFAULT_POINTING = _abi.POINTING_CERTIFIED
 
 
 # ---------------------------------------------------------------------------
@@ -576,6 +580,7 @@ class ProjEngBase:
         p.tiled = 1 if self._tiled else 0
         p.interp = _abi.INTERP_BILINEAR if self._bilinear else _abi.INTERP_NEAREST
         p.n_comp = self._ncomp
+        p.pointing = getattr(self, "pointing", DEFAULT_POINTING)
         if self._hp:
             p.nside = self.nside
             p.nest = 1 if self.nest else 0
