@@ -485,6 +485,30 @@ __device__ __forceinline__ void record_pixel_range(int *err, int tile, int det, 
     }
 }
 
+// float -> double by integer operations: exact, and no float64-pipe
+// instruction (GB300 runs float<->double conversions on its slow float64
+// pipe, at ~0.7 per clock per SM).
+__device__ __forceinline__ double f2d(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned s = u & 0x80000000u, ef = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+    // Subnormal floats: normalise the mantissa (leading one at bit p).
+    const int p = 31 - __clz(m | 1u);
+    const unsigned mn = (m << (23 - p)) & 0x7fffffu;
+    unsigned ed, mant;
+    if (ef == 0u) {
+        ed = m ? (unsigned)(p - 149 + 1023) : 0u;
+        mant = m ? mn : 0u;
+    } else if (ef == 255u) {
+        ed = 2047u;
+        mant = m;
+    } else {
+        ed = ef - 127u + 1023u;
+        mant = m;
+    }
+    const unsigned hw = s | (ed << 20) | (mant >> 3), lw = mant << 29;
+    return __hiloint2double((int)hw, (int)lw);
+}
+
 // Compensated float32 addition (Knuth's TwoSum): s + e == a + b exactly.
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
     s = a + b;
@@ -527,7 +551,7 @@ __device__ __forceinline__ void flush_runs(long long key, long long plane, float
     if (head && key >= 0) {
 #pragma unroll
         for (int k = 0; k < NV; k++)
-            if ((vmask >> k) & 1u) atomicAdd(map + key + mult[k] * plane, (double)v[k] + (double)e[k]);
+            if ((vmask >> k) & 1u) atomicAdd(map + key + mult[k] * plane, f2d(v[k]) + f2d(e[k]));
     }
 }
 

@@ -95,17 +95,30 @@ __global__ void __launch_bounds__(kBlock) k_from_map(GatherArgs a) {
             const double *bp = a.bore + 4LL * t;
             const double2 lo = __ldg(reinterpret_cast<const double2 *>(bp));
             const double2 hi = __ldg(reinterpret_cast<const double2 *>(bp) + 1);
-            const dfl qb[4] = {df_from_double(lo.x), df_from_double(lo.y), df_from_double(hi.x),
-                               df_from_double(hi.y)};
+            dfl qb[4];
+            bool ok = df_split(lo.x, qb[0]) & df_split(lo.y, qb[1]) & df_split(hi.x, qb[2]) &
+                      df_split(hi.y, qb[3]);
             int pix[NT][3];
-            float w[NT] = {1.f};
             float pf[3];
             bool on = false;
-            if (fast_car<P>(a.g, a.ft, a.fc, qb, qd, nc, T, Pr, pix[0], &on, pf)) {
-                if (on) gather_taps<P, NT>(a, a.signal + det * a.sig_stride + t, 1, pix, w, pf);
-            } else {
-                s_queue[atomicAdd(&s_qn, 1)] = t;
+            ok = ok && fast_car<P>(a.g, a.ft, a.fc, qb, qd, nc, T, Pr, pix[0], &on, pf);
+            if (ok && on) {
+                long long off, plane;
+                const int bad = locate<P>(a.g, pix[0], &off, &plane);
+                if (bad >= 0) {
+                    record_missing_tile(a.err, bad);
+                } else {
+                    // src/Projection.cxx:1763-1765 with certified float32
+                    // roundings (nearest neighbour: weight 1).
+                    float *sp = a.signal + det * a.sig_stride + t;
+                    float s = *sp;
+#pragma unroll
+                    for (int c = 0; c < 3; c++)
+                        if (ok && c < nc) ok = fast_accum(s, __ldg(a.map + off + c * plane), pf[c]);
+                    if (ok) *sp = s;
+                }
             }
+            if (!ok) s_queue[atomicAdd(&s_qn, 1)] = t;
         }
         __syncthreads();
         const int qn = s_qn;

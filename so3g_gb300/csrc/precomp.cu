@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(kBlock) k_pc_scatter(PcArgs a) {
         } else if (off >= 0) {
 #pragma unroll
             for (int k = 0; k < NV; k++)
-                if ((vmask >> k) & 1u) atomicAdd(a.map + off + mult[k] * plane, (double)v[k]);
+                if ((vmask >> k) & 1u) atomicAdd(a.map + off + mult[k] * plane, f2d(v[k]));
         }
     }
 }

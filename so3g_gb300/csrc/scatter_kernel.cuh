@@ -117,7 +117,7 @@ __device__ void exact_sample(const ScatterArgs &a, int det, int t, const QuatD &
         tap_values<WEIGHT>(sig, pf, w[k], det_wt, v);
 #pragma unroll
         for (int s = 0; s < NV; s++)
-            if ((vmask >> s) & 1u) atomicAdd(a.map + off + mult[s] * plane, (double)v[s]);
+            if ((vmask >> s) & 1u) atomicAdd(a.map + off + mult[s] * plane, f2d(v[s]));
     }
 }
 
@@ -165,10 +165,11 @@ __global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs a) {
                 const double *bp = a.bore + 4LL * t;
                 const double2 lo = __ldg(reinterpret_cast<const double2 *>(bp));
                 const double2 hi = __ldg(reinterpret_cast<const double2 *>(bp) + 1);
-                const dfl qb[4] = {df_from_double(lo.x), df_from_double(lo.y),
-                                   df_from_double(hi.x), df_from_double(hi.y)};
+                dfl qb[4];
+                bool ok = df_split(lo.x, qb[0]) & df_split(lo.y, qb[1]) &
+                          df_split(hi.x, qb[2]) & df_split(hi.y, qb[3]);
                 bool on = false;
-                if (fast_car<P>(a.g, a.ft, a.fc, qb, qd, nc, T, Pr, pix[0], &on, pf)) {
+                if (ok && fast_car<P>(a.g, a.ft, a.fc, qb, qd, nc, T, Pr, pix[0], &on, pf)) {
                     n = on ? 1 : 0;
                     w[0] = 1.f;
                 } else {
@@ -206,7 +207,7 @@ __global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs a) {
             } else if (off >= 0) {
 #pragma unroll
                 for (int s = 0; s < NV; s++)
-                    if ((vmask >> s) & 1u) atomicAdd(a.map + off + mult[s] * plane, (double)v[s]);
+                    if ((vmask >> s) & 1u) atomicAdd(a.map + off + mult[s] * plane, f2d(v[s]));
             }
         }
         if (kFastOK && fast) {

@@ -86,6 +86,35 @@ def test_certified_equals_exact_at_scale(tiled):
     assert res[1][on].min() < -0.99 and res[1][on].max() > 0.99
 
 
+def test_certified_from_map_accumulation_values():
+    """from_map adds map*pf to the signal in float64 and rounds to float32
+    after every term; the certified path reproduces that for signed zeros,
+    tiny and huge map values and a non-zero starting signal."""
+    import torch
+    Q, dets, resp, gamma, _ = synth.workload(16, 50_000, seed=13, radius_deg=0.5)
+    p, eng = _engine((300, 400), ARCMIN, False)
+    q = synth.native(p, Q)
+    rng = np.random.default_rng(3)
+    m = rng.standard_normal((3, 300, 400))
+    pick = rng.random(m.shape)
+    m[pick < 0.05] = 0.0
+    m[(pick >= 0.05) & (pick < 0.1)] = -0.0
+    m[(pick >= 0.1) & (pick < 0.15)] *= 1e-30
+    m[(pick >= 0.15) & (pick < 0.2)] *= 1e30
+    m[(pick >= 0.2) & (pick < 0.25)] = np.round(m[(pick >= 0.2) & (pick < 0.25)] * 8) / 8
+    sig0 = rng.standard_normal((16, 50_000)).astype(np.float32)
+    sig0[:, ::7] = 0.0
+    sig0[:, 1::7] = -0.0
+    qd, dd, rd, md = (torch.from_numpy(x).cuda() for x in (q, dets, resp, m))
+    out = []
+    for mode in (_abi.POINTING_EXACT, _abi.POINTING_CERTIFIED):
+        eng.pointing = mode
+        s = torch.from_numpy(sig0.copy()).cuda()
+        eng.from_map(md, qd, dd, rd, s)
+        out.append(s.cpu().numpy())
+    assert bits_equal(out[0], out[1])
+
+
 def test_certified_to_map_matches_exact():
     import torch
     Q, dets, resp, gamma, sig = synth.workload(64, 100_000, seed=12, radius_deg=1.0)
