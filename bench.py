@@ -36,6 +36,18 @@ sys.path.insert(0, ROOT)
 CONFIGS = {
     "cfg1": dict(n_det=64, n_time=100_000, radius=1.0, shape=(600, 600), noise=False),
     "cfg2": dict(n_det=1000, n_time=1_000_000, radius=1.5, shape=(2000, 2000), noise=True),
+    # HEALPix TQU nside 1024 RING (--tiled: NEST, nside_tile 16, every tile
+    # present); el 45, az 180 +- 30 deg at 2 deg/s drifting 15 deg/hour.
+    "cfg3": dict(kind="hp", n_det=2000, n_time=2_000_000, radius=1.5, nside=1024,
+                 nside_tile=16, el=45., throw=30., v_az=2., drift=15., noise=False),
+    # Differentiable from_map: ZEA bilinear TQU 3 x 3000 x 3000 at 0.5 arcmin,
+    # a Gaussian field with power ~ l^-2; one step = from_map forward +
+    # to_map backward through torch.autograd.
+    "cfg5": dict(kind="zea_grad", n_det=4000, n_time=2_000_000, radius=1.5,
+                 shape=(3000, 3000), res_arcmin=0.5, noise=False),
+    # 16 observations of uneven size into one CAR 3 x 4000 x 4000 map.
+    "cfg4": dict(n_obs=16, n_det=(500, 2000), n_time=(200_000, 2_000_000), el=(40., 60.),
+                 az_spread=90., radius=1.5, shape=(4000, 4000), res_arcmin=1.8, noise=False),
 }
 METRIC = "to_map/from_map TOD samples/s (CAR TQU) mixed vs FP64 GPU path, % HBM peak"
 ARCMIN = np.pi / 180 / 60
@@ -55,16 +67,46 @@ def parse():
     ap.add_argument("--no-fp64-path", action="store_true")
     ap.add_argument("--ops", default="to_map,from_map",
                     help="operations timed in a step (profiling runs pick one)")
+    ap.add_argument("--batch-scale", type=float, default=1.0,
+                    help="cfg4: scale every observation's sample count")
+    ap.add_argument("--tiled", action="store_true", help="cfg3: the Tiled NEST variant")
     return ap.parse_args()
 
 
 def config(args):
     c = dict(CONFIGS[args.config])
+    c.setdefault("kind", "car")
     if args.n_det:
         c["n_det"] = args.n_det
     if args.n_time:
         c["n_time"] = args.n_time
+    if args.tiled and c["kind"] == "hp":
+        c["tiled"] = True
     return c
+
+
+def describe(c):
+    """(metric, workload name, map shape) of a configuration."""
+    n = "%d det x %d samples" % (c["n_det"], c["n_time"])
+    if c["kind"] == "hp":
+        npix = 12 * c["nside"] ** 2
+        if c.get("tiled"):
+            w = "HEALPix TQU Tiled NEST nside %d (nside_tile %d) float64 map, %s" % (
+                c["nside"], c["nside_tile"], n)
+        else:
+            w = "HEALPix TQU NonTiled RING nside %d float64 map, %s" % (c["nside"], n)
+        return ("to_map/from_map TOD samples/s (HEALPix TQU)", w, [3, npix])
+    shape = list(c["shape"])
+    if c["kind"] == "zea_grad":
+        return ("differentiable from_map forward+backward TOD samples/s (ZEA bilinear TQU)",
+                "ZEA bilinear TQU NonTiled %dx%d float64 map, %s" % (shape[0], shape[1], n),
+                [3] + shape)
+    return (METRIC, "CAR TQU NonTiled %dx%d float64 map, %s" % (shape[0], shape[1], n),
+            [3] + shape)
+
+
+def npix_of(c):
+    return 12 * c["nside"] ** 2 if c["kind"] == "hp" else c["shape"][0] * c["shape"][1]
 
 
 def peaks():
@@ -79,12 +121,48 @@ def peaks():
 def host_inputs(c, seed=0):
     """Boresight (native frame), detectors, responses and the geometry."""
     from so3g_gb300 import synth
+    from so3g_gb300.proj.wcs import ProjectionistHealpix
     rng = np.random.default_rng(seed)
     dets, resp, gamma = synth.focal_plane(rng, c["n_det"], c["radius"])
-    Q, t = synth.scan(c["n_time"], rate=200., el=50., az0=180., throw=10., v_az=1.)
-    p = synth.car_projectionist(c["shape"], ARCMIN, el=50., az0=180.)
+    el = c.get("el", 50.)
+    Q, t = synth.scan(c["n_time"], rate=200., el=el, az0=180., throw=c.get("throw", 10.),
+                      v_az=c.get("v_az", 1.), drift_deg_per_hour=c.get("drift", 0.))
+    kind = c.get("kind", "car")
+    if kind == "hp":
+        if c.get("tiled"):
+            nt = 12 * c["nside_tile"] ** 2
+            p = ProjectionistHealpix.for_healpix(c["nside"], nside_tile=c["nside_tile"],
+                                                 active_tiles=list(range(nt)), ordering="NEST")
+        else:
+            p = ProjectionistHealpix.for_healpix(c["nside"], ordering="RING")
+    elif kind == "zea_grad":
+        p = synth.car_projectionist(c["shape"], c["res_arcmin"] * ARCMIN, el=el, az0=180.,
+                                    proj="ZEA", interpol="bilinear")
+    else:
+        p = synth.car_projectionist(c["shape"], c.get("res_arcmin", 1.) * ARCMIN, el=el,
+                                    az0=180.)
     q = synth.native(p, Q)
     return p, q, dets, resp
+
+
+def gaussian_field(torch, shape, dev, seed=0):
+    """(3, ny, nx) float64 Gaussian random field with power ~ l^-2."""
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    ny, nx = shape
+    w = torch.randn((3, ny, nx), generator=g, device=dev, dtype=torch.float64)
+    ky = torch.fft.fftfreq(ny, device=dev, dtype=torch.float64)[:, None]
+    kx = torch.fft.rfftfreq(nx, device=dev, dtype=torch.float64)[None, :]
+    ell = torch.sqrt(ky * ky + kx * kx)
+    amp = 1.0 / torch.clamp(ell, min=1.0 / max(ny, nx))
+    f = torch.fft.irfft2(torch.fft.rfft2(w) * amp, s=(ny, nx))
+    return (f / f.std()).contiguous()
+
+
+def zero_map(m):
+    for t in (m if isinstance(m, list) else [m]):
+        if t is not None:
+            t.zero_()
 
 
 def make_signal(torch, c, dev, seed=0):
@@ -161,10 +239,10 @@ class ClockSampler:
 
 def algorithmic_bytes(c, op):
     """Compulsory bytes per (det, sample) of an operation (map of
-    3 x ny x nx float64)."""
+    3 x npix float64)."""
     n_det, n_time = c["n_det"], c["n_time"]
     N = n_det * n_time
-    npix = c["shape"][0] * c["shape"][1]
+    npix = npix_of(c)
     bore = 32. / n_det
     dets = 16. / n_time
     if op == "to_map":
@@ -173,6 +251,9 @@ def algorithmic_bytes(c, op):
         return 8. + bore + dets + 8. * 3 * npix / N   # signal read + write
     if op == "to_weight_map":
         return bore + dets + 16. * 6 * npix / N
+    if op == "from_map_fwd_bwd":
+        # from_map (signal out) + to_map of the signal gradient
+        return algorithmic_bytes(c, "from_map") - 4. + algorithmic_bytes(c, "to_map")
     raise ValueError(op)
 
 
@@ -193,18 +274,30 @@ def run_ours(args, c, rank, world):
     dets_d = torch.from_numpy(dets).to(dev)
     resp_d = torch.from_numpy(resp).to(dev)
     sig = make_signal(torch, c, dev, seed=rank)
-    ny, nx = c["shape"]
-    m = torch.zeros((3, ny, nx), dtype=torch.float64, device=dev)
-    w = torch.zeros((3, 3, ny, nx), dtype=torch.float64, device=dev)
+    m = eng.zeros(3, device=dev)
+    w = eng.zeros((3, 3), device=dev)
     out = torch.zeros_like(sig)
     N = c["n_det"] * c["n_time"]
     ops = args.ops.split(",")
     stream = torch.cuda.current_stream()
+    if c["kind"] == "zea_grad":
+        from so3g_gb300 import autograd
+        field = gaussian_field(torch, c["shape"], dev, seed=rank)
+        ops = ["from_map_fwd_bwd"]
 
     def step(accum, ev=None):
         t = {}
+        if "from_map_fwd_bwd" in ops:
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            mm = field.detach().requires_grad_(True)
+            e0.record(stream)
+            s_ = autograd.from_map(eng, mm, q_d, dets_d, resp_d)
+            s_.backward(sig)
+            e1.record(stream)
+            t["from_map_fwd_bwd"] = (e0, e1)
         if "to_map" in ops:
-            m.zero_()
+            zero_map(m)
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
@@ -253,7 +346,7 @@ def run_ours(args, c, rank, world):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     res = {"ms_per_step": ms, "op_ms": op_ms, "launches": launches, "clocks": clocks}
-    if not args.no_fp64_path and world == 1:
+    if not args.no_fp64_path and world == 1 and c["kind"] == "car":
         # The plain float64 GPU path: exact float64 pointing, one float64
         # atomic per term.
         ms64, op64, _, _ = timed(_abi.ACCUM_ATOMIC, max(1, args.steps // 2), 1,
@@ -263,7 +356,7 @@ def run_ours(args, c, rank, world):
     # to_weight_map, timed on its own (not part of the step).
     if world == 1:
         for _ in range(2):
-            w.zero_()
+            zero_map(w)
             eng.to_weight_map(w, q_d, dets_d, resp_d, None, None)
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -273,7 +366,7 @@ def run_ours(args, c, rank, world):
         e1.record(stream)
         torch.cuda.synchronize()
         res["to_weight_map_ms"] = e0.elapsed_time(e1)
-    if not args.no_e2e and world == 1:
+    if not args.no_e2e and world == 1 and c["kind"] == "car":
         res["e2e"] = run_e2e(args, c, eng, q, dets, resp, sig, dev)
     del sig, out
     return res, N
@@ -317,6 +410,134 @@ def run_e2e(args, c, eng, q, dets, resp, sig_dev, dev):
 
 
 # ---------------------------------------------------------------------------
+# Batched map-making input: many observations into one map.
+
+def batch_inputs(c, scale=1.0, seed=0):
+    """Projectionist and per-observation host inputs (boresight in the
+    map's native frame, detectors, responses) of the batched workload."""
+    from so3g_gb300 import synth
+    rng = np.random.default_rng(seed)
+    ny, nx = c["shape"]
+    p = synth.car_projectionist((ny, nx), c["res_arcmin"] * ARCMIN, el=50., az0=180.)
+    obs = []
+    for i in range(c["n_obs"]):
+        nd = int(rng.integers(c["n_det"][0], c["n_det"][1] + 1))
+        nt = max(1, int(int(rng.integers(c["n_time"][0], c["n_time"][1] + 1)) * scale))
+        el = float(rng.uniform(*c["el"]))
+        az0 = 180. + float(rng.uniform(-0.5, 0.5)) * c["az_spread"]
+        dets, resp, _ = synth.focal_plane(rng, nd, c["radius"])
+        Q, _ = synth.scan(nt, rate=200., el=el, az0=az0, throw=10., v_az=1.)
+        obs.append((synth.native(p, Q), dets, resp))
+    return p, obs
+
+
+def run_batch(args, c):
+    """One step = to_map + to_weight_map of every observation into one
+    map (zeroed first), as one CUDA graph of two persistent batched
+    launches with autotuned launch shapes; compared against one plain
+    to_map + to_weight_map call per observation."""
+    import torch
+    from so3g_gb300 import _abi
+    from so3g_gb300.batch import Observation, ObservationBatch
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    lib = _abi.lib()
+    p, hobs = batch_inputs(c, args.batch_scale)
+    eng = p.get_ProjEng("TQU")
+    g = torch.Generator(device=dev)
+    g.manual_seed(0)
+    obs = []
+    for q, dets, resp in hobs:
+        sig = torch.randn((dets.shape[0], q.shape[0]), generator=g, device=dev,
+                          dtype=torch.float32)
+        obs.append(Observation(torch.from_numpy(q).to(dev), torch.from_numpy(dets).to(dev),
+                               torch.from_numpy(resp).to(dev), sig))
+    N = sum(o.signal.numel() for o in obs)
+    b = ObservationBatch(eng, obs)
+    tune = {}
+    for weight in (False, True):
+        piece, blocks = b.tune(weight=weight, pieces=(4096, 8192, 16384, 32768),
+                               blocks_per_sm=(0, 2), reps=1, store=False)
+        tune["to_weight_map" if weight else "to_map"] = {
+            "piece": piece, "blocks": blocks, "log": b.tune_log}
+    ny, nx = c["shape"]
+    m = torch.zeros((3, ny, nx), dtype=torch.float64, device=dev)
+    w = torch.zeros((3, 3, ny, nx), dtype=torch.float64, device=dev)
+    t_m, t_w = tune["to_map"], tune["to_weight_map"]
+    graph = b.graph(m, w, map_shape=(t_m["piece"], t_m["blocks"]),
+                    weight_shape=(t_w["piece"], t_w["blocks"]))
+    stream = torch.cuda.current_stream()
+
+    def step():
+        m.zero_()
+        w.zero_()
+        graph.replay()
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with ClockSampler(dev.index) as clk:
+            e0.record(stream)
+            for _ in range(steps):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps, clk.summary()
+
+    ms, clocks = timed(step, args.steps, args.warmup)
+    graph.check()
+    m_batch = m.clone()
+
+    def sequential():
+        m.zero_()
+        w.zero_()
+        for o in obs:
+            eng.to_map(m, o.boresight, o.dets, o.response, o.signal, None, None)
+            eng.to_weight_map(w, o.boresight, o.dets, o.response, None, None)
+
+    n0 = lib.so3g_launch_count()
+    ms_seq, _ = timed(sequential, max(1, args.steps // 2), 1)
+    seq_launches = (lib.so3g_launch_count() - n0) // (max(1, args.steps // 2) + 1)
+    err = float((m - m_batch).abs().max() / m_batch.abs().max())
+
+    # to_map batch alone, for the roofline.
+    def to_map_only():
+        b.to_map(m, piece=t_m["piece"], blocks=t_m["blocks"])
+    ms_tm, _ = timed(to_map_only, 2, 1)
+    npix = ny * nx
+    bytes_tm = sum(4. * o.signal.numel() + 32. * o.boresight.shape[0] + 16. * o.dets.shape[0]
+                   for o in obs) + 16. * 3 * npix
+    hbm, kind = peaks()
+    achieved = bytes_tm / (ms_tm * 1e-3) / 1e9
+    sizes = [[int(o.dets.shape[0]), int(o.boresight.shape[0])] for o in obs]
+    cfg = {"workload": "16 observations (det 500-2000, samples 200k-2M) into one CAR TQU "
+                       "3x%dx%d float64 map" % (ny, nx),
+           "n_obs": len(obs), "samples": N, "sizes": sizes, "batch_scale": args.batch_scale,
+           "step": "to_map + to_weight_map, one CUDA graph of two persistent launches",
+           "l2": "inputs larger than L2 (TOD %.1f GB)" % (N * 4 / 1e9),
+           "parallelism": "single GPU"}
+    line = {"metric": "batched to_map + to_weight_map TOD samples/s (CAR TQU, 16 obs)",
+            "value": N / (ms * 1e-3), "unit": "samples/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": cfg, "tuned": {k: {"piece": v["piece"], "blocks": v["blocks"]}
+                                     for k, v in tune.items()},
+            "tune_log": {k: v["log"] for k, v in tune.items()},
+            "sequential": {"value": N / (ms_seq * 1e-3), "ms_per_step": ms_seq,
+                           "launches_per_step": int(seq_launches),
+                           "batched_speedup": ms_seq / ms,
+                           "max_rel_map_diff": err},
+            "roofline": {"bound": "hbm", "kernel": "to_map batch", "achieved": achieved,
+                         "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                         "peak_kind": kind, "to_map_ms": ms_tm},
+            "clocks": clocks, "gpu_launches": graph.launches * args.steps}
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
 # CPU: the oracle (the reference's algorithm restated in C++ with OpenMP).
 
 def cpu_sample(c, n_det_s, n_time_s):
@@ -333,19 +554,20 @@ def run_cpu(c, n_det_s, n_time_s, steps=1, threads=None):
     nthreads = threads or os.cpu_count() or 1
     orc.set_threads(nthreads)
     s = cpu_sample(c, n_det_s, n_time_s)
+    s["tiled"] = False        # the oracle runs the untiled map
     p, q, dets, resp = host_inputs(s)
     eng = p.get_ProjEng("TQU")
     pz = eng._pz()
     rng = np.random.default_rng(0)
     sig = rng.standard_normal((n_det_s, n_time_s), dtype=np.float32)
-    ny, nx = c["shape"]
+    npix = npix_of(c)
     t0 = time.perf_counter()
     lab = orc.labels(pz, q, dets, 0, nthreads)
     t_assign = time.perf_counter() - t0
     threads_ranges = _labels_to_threads(lab, nthreads)
     best = None
     for _ in range(steps):
-        m = np.zeros(3 * ny * nx)
+        m = np.zeros(3 * npix)
         t0 = time.perf_counter()
         orc.to_map(pz, q, dets, resp, sig, None, m, threads=threads_ranges)
         t1 = time.perf_counter()
@@ -402,6 +624,8 @@ def cpu_sample_size(c):
 
 def main():
     args = parse()
+    if args.config == "cfg4" and args.impl == "ours":
+        return run_batch(args, dict(CONFIGS["cfg4"]))
     c = config(args)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -410,13 +634,15 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         dist.init_process_group("nccl")
-    workload = "CAR TQU NonTiled %dx%d float64 map, %d det x %d samples" % (
-        c["shape"][0], c["shape"][1], c["n_det"], c["n_time"])
+    metric, workload, map_shape = describe(c)
+    step_name = ("from_map forward + to_map backward (torch.autograd)"
+                 if c["kind"] == "zea_grad" else args.ops.replace(",", " + "))
     cfg = {"workload": workload, "n_det": c["n_det"], "n_time": c["n_time"],
-           "map": [3] + list(c["shape"]), "step": args.ops.replace(",", " + "),
+           "map": map_shape, "step": step_name,
            "l2": "inputs larger than L2 (TOD %.1f GB)" % (c["n_det"] * c["n_time"] * 4 / 1e9),
-           "precision": "pointing certified equal to float64 (double-float with float64 "
-                        "fallback), float32 products, float64 map accumulation",
+           "precision": ("pointing certified equal to float64 (double-float with float64 "
+                         "fallback)" if c["kind"] == "car" else "float64 pointing") +
+                        ", float32 products, float64 map accumulation",
            "parallelism": "replicas" if world > 1 else "single GPU"}
 
     if args.impl == "reference":
@@ -424,7 +650,7 @@ def main():
             return
         nd, nt = cpu_sample_size(c)
         r = run_cpu(c, nd, nt, steps=max(1, args.steps))
-        line = {"metric": METRIC, "value": r["value"], "unit": "samples/s", "n_gpus": world,
+        line = {"metric": metric, "value": r["value"], "unit": "samples/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step":
                 c["n_det"] * c["n_time"] / r["value"] * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -447,7 +673,7 @@ def main():
     op = "to_map" if "to_map" in res["op_ms"] else list(res["op_ms"])[0]
     B = algorithmic_bytes(c, op)
     achieved = B * N / (res["op_ms"][op] * 1e-3) / 1e9
-    line = {"metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world,
+    line = {"metric": metric, "value": value, "unit": "samples/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": cfg,

@@ -298,6 +298,46 @@ int so3g_proj_to_weight_map(const so3g_pixelization *pz,
                             const so3g_map *map,
                             int32_t accum, int32_t *err, void *stream);
 
+/* ---- Batches of observations --------------------------------------------
+ * Many observations (each its own boresight, focal plane and signal)
+ * projected into one map by one persistent launch: the work items
+ * (observation, detector, piece of `piece` samples) of all observations
+ * are shared out over `blocks` resident blocks.  A caller projecting N
+ * observations with so3g_proj_to_map makes N launches; the reference
+ * makes N calls of ProjectionEngine::to_map (src/Projection.cxx:1924-1966).
+ * The sums are the same; only the float64 summation order differs. */
+typedef struct so3g_obs {
+    const double *boresight;    /* device (n_time, 4) */
+    const double *dets;         /* device (n_det, 4) */
+    const float  *response;     /* device (n_det, 2) */
+    const float  *signal;       /* device rows (to_map), NULL otherwise */
+    const float  *det_weights;  /* device (n_det,), or NULL */
+    int64_t       sig_det_stride;
+    int32_t       n_time;
+    int32_t       n_det;
+} so3g_obs;
+
+/* Host helper: work_offset[o] = number of work items of observations
+ * 0..o-1 (n_det * ceil(n_time / piece) each), for o = 0..n_obs; returns
+ * the total.  obs is read on the host (only n_time and n_det). */
+int64_t so3g_batch_work_offsets(const so3g_obs *obs, int32_t n_obs, int32_t piece,
+                                int64_t *work_offset);
+
+/* to_map / to_weight_map of a batch.  obs (n_obs entries) and work_offset
+ * (n_obs + 1 entries, from so3g_batch_work_offsets with the same piece)
+ * are DEVICE arrays.  blocks <= 0 launches one full wave (as many blocks
+ * as fit on the device at once). */
+int so3g_proj_to_map_batch(const so3g_pixelization *pz, const so3g_obs *obs,
+                           int32_t n_obs, const int64_t *work_offset,
+                           int64_t n_work, int32_t piece, int32_t blocks,
+                           const so3g_map *map, int32_t accum, int32_t *err,
+                           void *stream);
+int so3g_proj_to_weight_map_batch(const so3g_pixelization *pz, const so3g_obs *obs,
+                                  int32_t n_obs, const int64_t *work_offset,
+                                  int64_t n_work, int32_t piece, int32_t blocks,
+                                  const so3g_map *map, int32_t accum, int32_t *err,
+                                  void *stream);
+
 /* ProjectionEngine::from_map (src/Projection.cxx:1728-1770):
  *   sig += map[c, pix] * pf[c] * w, rounded to float32 after every term;
  * accumulates into `signal`. */

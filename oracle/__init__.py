@@ -137,13 +137,23 @@ class Oracle:
         self._check(self.lib.orc_coords(ctypes.byref(pz), _p(bore), nt, _p(dets), nd, _p(out)))
         return out
 
+    @staticmethod
+    def _check_index_count(pz, index_count):
+        """Pixel index entries per sample: 1 (+1 tiled) for HEALPix, 2 (+1
+        tiled) for flat maps; the C side writes that many."""
+        want = (1 if pz.pix_sys == 1 else 2) + (1 if pz.tiled else 0)
+        if index_count != want:
+            raise ValueError("index_count %d; this pixelization has %d" % (index_count, want))
+
     def pixels(self, pz, bore, dets, index_count):
+        self._check_index_count(pz, index_count)
         bore, dets, nt, nd = self._in(bore, dets)
         out = np.zeros((nd, nt, index_count), dtype=np.int32)
         self._check(self.lib.orc_pixels(ctypes.byref(pz), _p(bore), nt, _p(dets), nd, _p(out)))
         return out
 
     def pointing_matrix(self, pz, bore, dets, resp, index_count):
+        self._check_index_count(pz, index_count)
         bore, dets, nt, nd = self._in(bore, dets)
         resp = np.ascontiguousarray(resp, dtype=np.float32)
         pix = np.zeros((nd, nt, index_count), dtype=np.int32)

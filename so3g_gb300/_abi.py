@@ -72,6 +72,19 @@ class PrecompGeom(ctypes.Structure):
     ]
 
 
+class Obs(ctypes.Structure):
+    _fields_ = [
+        ("boresight", c_void_p),
+        ("dets", c_void_p),
+        ("response", c_void_p),
+        ("signal", c_void_p),
+        ("det_weights", c_void_p),
+        ("sig_det_stride", c_int64),
+        ("n_time", c_int32),
+        ("n_det", c_int32),
+    ]
+
+
 P = ctypes.POINTER
 _SIGS = {
     "so3g_init": (ctypes.c_int, []),
@@ -105,6 +118,13 @@ _SIGS = {
     "so3g_proj_from_map": (ctypes.c_int, [P(Pixelization), c_void_p, c_int32, c_void_p, c_int32,
                                           c_void_p, P(Map), c_void_p, c_int64, c_void_p,
                                           c_void_p]),
+    "so3g_batch_work_offsets": (c_int64, [P(Obs), c_int32, c_int32, c_void_p]),
+    "so3g_proj_to_map_batch": (ctypes.c_int, [P(Pixelization), c_void_p, c_int32, c_void_p,
+                                              c_int64, c_int32, c_int32, P(Map), c_int32,
+                                              c_void_p, c_void_p]),
+    "so3g_proj_to_weight_map_batch": (ctypes.c_int, [P(Pixelization), c_void_p, c_int32,
+                                                     c_void_p, c_int64, c_int32, c_int32,
+                                                     P(Map), c_int32, c_void_p, c_void_p]),
     "so3g_precomp_to_map": (ctypes.c_int, [P(PrecompGeom), c_void_p, c_void_p, c_int32, c_int32,
                                            c_void_p, c_int64, c_void_p, P(Ranges), P(Map),
                                            c_int32, c_void_p, c_void_p]),

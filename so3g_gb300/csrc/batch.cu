@@ -1,0 +1,159 @@
+// batch.cu -- to_map / to_weight_map of many observations into one map in
+// one persistent launch.
+//
+// The work items of all observations -- (observation, piece of `piece`
+// samples, detector), numbered observation by observation and piece by
+// piece -- are shared out
+// statically over the resident blocks (item w goes to block w mod
+// gridDim.x).  Each item runs the same per-piece code as so3g_proj_to_map.
+
+#include "scatter_kernel.cuh"
+
+namespace so3g {
+
+namespace {
+
+template <int C, int P, bool WEIGHT>
+__global__ void __launch_bounds__(kBlock)
+    k_scatter_batch(ScatterArgs base, const so3g_obs *obs, int n_obs,
+                    const long long *work_off, long long n_work) {
+    __shared__ int s_queue[FastEligible<C, P>::value ? kQueueCap : 1];
+    __shared__ int s_qn;
+    for (long long w = blockIdx.x; w < n_work; w += gridDim.x) {
+        // The observation holding item w: largest o with work_off[o] <= w.
+        int lo = 0, hi = n_obs - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(work_off + mid) <= w) lo = mid;
+            else hi = mid - 1;
+        }
+        const so3g_obs ob = obs[lo];
+        const long long item = w - __ldg(work_off + lo);
+        const int pieces = (ob.n_time + base.piece - 1) / base.piece;
+        if (pieces <= 0 || ob.n_det <= 0) continue;   // never for a consistent plan
+        // Piece-major: consecutive items are different detectors over the
+        // same samples, so the blocks running at once spread their atomics
+        // over the focal plane's footprint instead of one detector's track.
+        const int pc = (int)(item / ob.n_det);
+        const int det = (int)(item - (long long)pc * ob.n_det);
+        const int t0 = pc * base.piece;
+        const int t1 = min(ob.n_time, t0 + base.piece);
+        if (pc >= pieces || t0 >= t1) continue;   // never for a consistent plan
+        ScatterArgs a = base;
+        a.bore = ob.boresight;
+        a.dets = ob.dets;
+        a.resp = ob.response;
+        a.signal = ob.signal;
+        a.sig_stride = ob.sig_det_stride;
+        a.det_weights = ob.det_weights;
+        scatter_piece<C, P, WEIGHT>(a, det, t0, t1, s_queue, s_qn);
+    }
+}
+
+template <bool WEIGHT>
+struct BatchLaunch {
+    ScatterArgs a;
+    const so3g_obs *obs;
+    int n_obs;
+    const long long *work_off;
+    long long n_work;
+    int blocks;
+    cudaStream_t stream;
+    int sms;
+    template <int C, int P>
+    int run() {
+        int grid = blocks;
+        if (grid <= 0) {
+            // One full wave: every block resident at once.
+            int per_sm = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scatter_batch<C, P, WEIGHT>,
+                                                          kBlock, 0);
+            grid = (per_sm > 0 ? per_sm : 1) * sms;
+        }
+        if ((long long)grid > n_work) grid = (int)n_work;
+        k_scatter_batch<C, P, WEIGHT><<<grid, kBlock, 0, stream>>>(a, obs, n_obs, work_off,
+                                                                     n_work);
+        return after_launch(WEIGHT ? "to_weight_map batch" : "to_map batch");
+    }
+};
+
+template <bool WEIGHT>
+int batch_entry(const so3g_pixelization *pz, const so3g_obs *obs, int32_t n_obs,
+                const int64_t *work_offset, int64_t n_work, int32_t piece, int32_t blocks,
+                const so3g_map *map, int32_t accum, int32_t *err, void *stream) {
+    clear_error();
+    BatchLaunch<WEIGHT> L;
+    int rc = make_geom(pz, &L.a.g);
+    if (rc) return rc;
+    rc = attach_map(pz, map, &L.a.g);
+    if (rc) return rc;
+    if (accum != SO3G_ACCUM_ATOMIC && accum != SO3G_ACCUM_WARP_RUNS)
+        return set_error(SO3G_ERR_ARGUMENT, "unknown accumulation mode %d", accum);
+    if (n_obs < 0 || n_work < 0) return set_error(SO3G_ERR_ARGUMENT, "negative size");
+    if (n_obs == 0 || n_work == 0) return SO3G_OK;
+    if (!obs || !work_offset) return set_error(SO3G_ERR_ARGUMENT, "NULL observation table");
+    if (piece < 256 || piece % 256)
+        return set_error(SO3G_ERR_ARGUMENT, "piece must be a positive multiple of 256");
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    L.blocks = blocks;
+    L.sms = sms > 0 ? sms : 1;
+    L.a.bore = nullptr;
+    L.a.dets = nullptr;
+    L.a.resp = nullptr;
+    L.a.signal = nullptr;
+    L.a.sig_stride = 0;
+    L.a.det_weights = nullptr;
+    L.a.segs = Segs{nullptr, 0};
+    L.a.piece = piece;
+    L.a.accum = accum;
+    L.a.err = err;
+    L.a.map = map->data;
+    L.a.ft = device_fast_tables();
+    L.a.fc = make_fast_const(L.a.g);
+    L.a.fast = (pz->pointing == SO3G_POINTING_CERTIFIED && L.a.ft.asin_t) ? 1 : 0;
+    L.obs = obs;
+    L.n_obs = n_obs;
+    L.work_off = reinterpret_cast<const long long *>(work_offset);
+    L.n_work = n_work;
+    L.stream = (cudaStream_t)stream;
+    return dispatch_cp(pz->coord_sys, pix_kind(pz), L);
+}
+
+}  // namespace
+
+}  // namespace so3g
+
+extern "C" {
+
+int64_t so3g_batch_work_offsets(const so3g_obs *obs, int32_t n_obs, int32_t piece,
+                                int64_t *work_offset) {
+    if (!obs || !work_offset || n_obs < 0 || piece <= 0) return -1;
+    int64_t total = 0;
+    for (int o = 0; o < n_obs; o++) {
+        work_offset[o] = total;
+        const int64_t pieces = ((int64_t)obs[o].n_time + piece - 1) / piece;
+        total += (int64_t)obs[o].n_det * pieces;
+    }
+    work_offset[n_obs] = total;
+    return total;
+}
+
+int so3g_proj_to_map_batch(const so3g_pixelization *pz, const so3g_obs *obs, int32_t n_obs,
+                           const int64_t *work_offset, int64_t n_work, int32_t piece,
+                           int32_t blocks, const so3g_map *map, int32_t accum, int32_t *err,
+                           void *stream) {
+    return so3g::batch_entry<false>(pz, obs, n_obs, work_offset, n_work, piece, blocks, map,
+                                    accum, err, stream);
+}
+
+int so3g_proj_to_weight_map_batch(const so3g_pixelization *pz, const so3g_obs *obs,
+                                  int32_t n_obs, const int64_t *work_offset, int64_t n_work,
+                                  int32_t piece, int32_t blocks, const so3g_map *map,
+                                  int32_t accum, int32_t *err, void *stream) {
+    return so3g::batch_entry<true>(pz, obs, n_obs, work_offset, n_work, piece, blocks, map,
+                                   accum, err, stream);
+}
+
+}  // extern "C"

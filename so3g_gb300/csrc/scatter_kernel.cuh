@@ -121,13 +121,12 @@ __device__ void exact_sample(const ScatterArgs &a, int det, int t, const QuatD &
     }
 }
 
+// Samples [t0, t1) of detector `det`; every thread of the block calls it
+// with the same arguments.  s_queue/s_qn: the block's shared fallback queue.
 template <int C, int P, bool WEIGHT>
-__global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs a) {
+__device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int t0, int t1,
+                                              int *s_queue, int &s_qn) {
     constexpr bool kFastOK = FastEligible<C, P>::value;
-    __shared__ int s_queue[kFastOK ? kQueueCap : 1];
-    __shared__ int s_qn;
-    int det, t0, t1;
-    if (!seg_piece(a.segs, a.piece, det, t0, t1)) return;
     float det_wt = 1.f;
     if (a.det_weights) {
         det_wt = __ldg(a.det_weights + det);
@@ -223,6 +222,15 @@ __global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs a) {
             }
         }
     }
+}
+
+template <int C, int P, bool WEIGHT>
+__global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs a) {
+    __shared__ int s_queue[FastEligible<C, P>::value ? kQueueCap : 1];
+    __shared__ int s_qn;
+    int det, t0, t1;
+    if (!seg_piece(a.segs, a.piece, det, t0, t1)) return;
+    scatter_piece<C, P, WEIGHT>(a, det, t0, t1, s_queue, s_qn);
 }
 
 }  // namespace
