@@ -456,8 +456,8 @@ def run_batch(args, c):
     b = ObservationBatch(eng, obs)
     tune = {}
     for weight in (False, True):
-        piece, blocks = b.tune(weight=weight, pieces=(4096, 8192, 16384, 32768),
-                               blocks_per_sm=(0, 2), reps=1, store=False)
+        piece, blocks = b.tune(weight=weight, pieces=(8192, 32768),
+                               blocks_per_sm=(0, -1), reps=1, store=False)
         tune["to_weight_map" if weight else "to_map"] = {
             "piece": piece, "blocks": blocks, "log": b.tune_log}
     ny, nx = c["shape"]
@@ -516,7 +516,7 @@ def run_batch(args, c):
     cfg = {"workload": "16 observations (det 500-2000, samples 200k-2M) into one CAR TQU "
                        "3x%dx%d float64 map" % (ny, nx),
            "n_obs": len(obs), "samples": N, "sizes": sizes, "batch_scale": args.batch_scale,
-           "step": "to_map + to_weight_map, one CUDA graph of two persistent launches",
+           "step": "to_map + to_weight_map, one CUDA graph with the tuned launches",
            "l2": "inputs larger than L2 (TOD %.1f GB)" % (N * 4 / 1e9),
            "parallelism": "single GPU"}
     line = {"metric": "batched to_map + to_weight_map TOD samples/s (CAR TQU, 16 obs)",

@@ -325,8 +325,9 @@ int64_t so3g_batch_work_offsets(const so3g_obs *obs, int32_t n_obs, int32_t piec
 
 /* to_map / to_weight_map of a batch.  obs (n_obs entries) and work_offset
  * (n_obs + 1 entries, from so3g_batch_work_offsets with the same piece)
- * are DEVICE arrays.  blocks <= 0 launches one full wave (as many blocks
- * as fit on the device at once). */
+ * are DEVICE arrays.  blocks > 0: a grid of that many blocks, each taking
+ * every blocks-th work item; 0: one full wave of resident blocks (as many
+ * as fit on the device at once); < 0: one block per work item. */
 int so3g_proj_to_map_batch(const so3g_pixelization *pz, const so3g_obs *obs,
                            int32_t n_obs, const int64_t *work_offset,
                            int64_t n_work, int32_t piece, int32_t blocks,

@@ -10,7 +10,8 @@ each call is a ProjectionEngine::to_map (src/Projection.cxx:1924-1966).
 launch: the work items (observation, detector, piece of ``piece`` samples)
 of the whole batch are shared out over one wave of resident blocks.
 
-* ``to_map`` / ``to_weight_map`` run one batched launch each.
+* ``to_map`` / ``to_weight_map`` run one batched launch each (or, when
+  the tuner finds it faster, one ordinary launch per observation).
 * ``tune`` times a small grid of (piece, blocks) launch shapes on scratch
   maps and keeps the fastest; results are cached in a JSON file keyed by
   device, pixelization and batch size (``SO3G_GB300_TUNE_CACHE`` names the
@@ -34,9 +35,13 @@ from .projeng import (_ErrRecord, _MapArg, _device, _ensure_init, _stream, as_ar
                       DEFAULT_ACCUM)
 
 # Launch shapes the tuner tries: samples per work item, and blocks per SM
-# (0 = one full wave, as many blocks as fit at once).
+# (0 = one persistent full wave, as many blocks as fit at once; -1 = one
+# block per work item).  PER_OBSERVATION, as the blocks value, stands for
+# one ordinary projection launch per observation instead of one batched
+# launch; the tuner tries it once.
 TUNE_PIECES = (2048, 4096, 8192, 16384, 32768)
-TUNE_BLOCKS_PER_SM = (0, 2, 4)
+TUNE_BLOCKS_PER_SM = (0, 2, 4, -1)
+PER_OBSERVATION = -2
 DEFAULT_PIECE = 8192
 
 
@@ -144,6 +149,25 @@ class ObservationBatch:
         return self._plans[piece]
 
     def _launch(self, weight, m, piece, blocks, accum):
+        acc = DEFAULT_ACCUM if accum is None else accum
+        if blocks == PER_OBSERVATION:
+            # One projection launch per observation (the piece is chosen by
+            # the library); captured in a graph, they replay as one.
+            lib, pz = _abi.lib(), self.eng._pz()
+            for r, (bore, dets, resp, w, sig) in zip(self._host_recs, self._keep):
+                if r.n_time == 0 or r.n_det == 0:
+                    continue
+                if weight:
+                    rc = lib.so3g_proj_to_weight_map(
+                        pz, r.boresight, r.n_time, r.dets, r.n_det, r.response, r.det_weights,
+                        None, m.struct, acc, self._err.ptr, _stream())
+                else:
+                    rc = lib.so3g_proj_to_map(
+                        pz, r.boresight, r.n_time, r.dets, r.n_det, r.response, r.signal,
+                        r.sig_det_stride, r.det_weights, None, m.struct, acc, self._err.ptr,
+                        _stream())
+                _abi.check(rc, "to_weight_map" if weight else "to_map")
+            return
         off, n_work = self.plan(piece)
         fn = (_abi.lib().so3g_proj_to_weight_map_batch if weight
               else _abi.lib().so3g_proj_to_map_batch)
@@ -206,9 +230,10 @@ class ObservationBatch:
         return None
 
     def tune(self, weight=False, pieces=TUNE_PIECES, blocks_per_sm=TUNE_BLOCKS_PER_SM,
-             reps=2, store=True):
+             reps=2, store=True, per_observation=True):
         """Times every (piece, blocks) candidate on a scratch map (after
-        one warm-up launch) and returns the fastest as (piece, blocks);
+        one warm-up launch), and one launch per observation when
+        ``per_observation``; returns the fastest as (piece, blocks) and
         stores it in the cache when ``store``.  The timings are in
         ``self.tune_log``."""
         eng = self.eng
@@ -217,18 +242,20 @@ class ObservationBatch:
         sms = torch.cuda.get_device_properties(_device()).multi_processor_count
         stream = torch.cuda.current_stream()
         log = []
-        self._launch(weight, m, pieces[0], blocks_per_sm[0] * sms, None)
-        for piece in pieces:
-            for bps in blocks_per_sm:
-                blocks = bps * sms
-                t0 = torch.cuda.Event(enable_timing=True)
-                t1 = torch.cuda.Event(enable_timing=True)
-                t0.record(stream)
-                for _ in range(reps):
-                    self._launch(weight, m, piece, blocks, None)
-                t1.record(stream)
-                t1.synchronize()
-                log.append({"piece": piece, "blocks": blocks, "ms": t0.elapsed_time(t1) / reps})
+        self._launch(weight, m, pieces[0], max(blocks_per_sm[0], 0) * sms, None)
+        shapes = [(piece, bps * sms if bps >= 0 else -1) for piece in pieces
+                  for bps in blocks_per_sm]
+        if per_observation:
+            shapes.append((DEFAULT_PIECE, PER_OBSERVATION))
+        for piece, blocks in shapes:
+            t0 = torch.cuda.Event(enable_timing=True)
+            t1 = torch.cuda.Event(enable_timing=True)
+            t0.record(stream)
+            for _ in range(reps):
+                self._launch(weight, m, piece, blocks, None)
+            t1.record(stream)
+            t1.synchronize()
+            log.append({"piece": piece, "blocks": blocks, "ms": t0.elapsed_time(t1) / reps})
         self._err.t.zero_()
         best = min(log, key=lambda r: r["ms"])
         self.tune_log = log
@@ -276,10 +303,12 @@ class BatchGraph:
         batch._err.t.zero_()
         torch.cuda.synchronize()
         self.graph = torch.cuda.CUDAGraph()
+        n0 = _abi.lib().so3g_launch_count()
         with torch.cuda.graph(self.graph):
             for weight, m, piece, blocks in launches:
                 batch._launch(weight, m, piece, blocks, accum)
-        self.launches = len(launches)
+        # Kernel launches recorded in the graph (each replay runs them all).
+        self.launches = int(_abi.lib().so3g_launch_count() - n0)
 
     def replay(self):
         self.graph.replay()

@@ -41,6 +41,17 @@ void fast_knots(const double *v, float4 *out) {
     }
 }
 
+// sin and cos of the asin table's knots as double-floats: the HEALPix
+// certified pointing evaluates sin/cos(lat) about the knot below lat.
+void sincos_knots(const double *v, float4 *out) {
+    for (int i = 0; i < kLutN; i++) {
+        float sh, sl, ch, cl;
+        split(std::sin(v[i]), sh, sl);
+        split(std::cos(v[i]), ch, cl);
+        out[i] = make_float4(sh, sl, ch, cl);
+    }
+}
+
 // asinTable / atan2Table construction (include/so_linterp.h:35-39, 51-56),
 // with the host math library, as the reference's static tables
 // (src/Projection.cxx:36-38).
@@ -84,11 +95,12 @@ const double *device_lut() {
 
 FastTables device_fast_tables() {
     int dev = 0;
-    FastTables t{nullptr, nullptr};
+    FastTables t{nullptr, nullptr, nullptr};
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return t;
     if (g_fast_lut[dev]) {
         t.asin_t = g_fast_lut[dev];
         t.atan2_t = g_fast_lut[dev] + kLutN;
+        t.asin_sc = g_fast_lut[dev] + 2 * kLutN;
     }
     return t;
 }
@@ -102,6 +114,9 @@ FastConst make_fast_const(const DGeom &g) {
     split(g.cry - 1 + 0.5, c.off_y.hi, c.off_y.lo);
     split(kPi, c.pi.hi, c.pi.lo);
     split(kPi / 2, c.half_pi.hi, c.half_pi.lo);
+    split(1. / (2. * kPi), c.inv_2pi.hi, c.inv_2pi.lo);
+    split(1. / 3., c.third.hi, c.third.lo);
+    split(2. / 3., c.two_thirds.hi, c.two_thirds.lo);
     return c;
 }
 
@@ -224,13 +239,14 @@ int so3g_init(void) {
     }
     g_lut[dev] = d;
     // Double-float knots for the certified pointing.
-    static float4 knots[2 * kLutN];
+    static float4 knots[3 * kLutN];
     fast_knots(g_host_lut, knots);
     fast_knots(g_host_lut + kLutN, knots + kLutN);
+    sincos_knots(g_host_lut, knots + 2 * kLutN);
     float4 *f = nullptr;
-    e = cudaMalloc(&f, sizeof(float4) * 2 * kLutN);
+    e = cudaMalloc(&f, sizeof(float4) * 3 * kLutN);
     if (e != cudaSuccess) return set_error(SO3G_ERR_CUDA, "cudaMalloc: %s", cudaGetErrorString(e));
-    e = cudaMemcpy(f, knots, sizeof(float4) * 2 * kLutN, cudaMemcpyHostToDevice);
+    e = cudaMemcpy(f, knots, sizeof(float4) * 3 * kLutN, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         cudaFree(f);
         return set_error(SO3G_ERR_CUDA, "cudaMemcpy: %s", cudaGetErrorString(e));

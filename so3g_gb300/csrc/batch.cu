@@ -14,7 +14,7 @@ namespace so3g {
 namespace {
 
 template <int C, int P, bool WEIGHT>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, kScatterBlocksPerSM)
     k_scatter_batch(ScatterArgs base, const so3g_obs *obs, int n_obs,
                     const long long *work_off, long long n_work) {
     __shared__ int s_queue[FastEligible<C, P>::value ? kQueueCap : 1];
@@ -62,17 +62,22 @@ struct BatchLaunch {
     int sms;
     template <int C, int P>
     int run() {
-        int grid = blocks;
-        if (grid <= 0) {
+        long long grid = blocks;
+        if (blocks < 0) {
+            // One block per work item, scheduled by the hardware.
+            grid = n_work;
+        } else if (blocks == 0) {
             // One full wave: every block resident at once.
             int per_sm = 0;
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scatter_batch<C, P, WEIGHT>,
                                                           kBlock, 0);
             grid = (per_sm > 0 ? per_sm : 1) * sms;
         }
-        if ((long long)grid > n_work) grid = (int)n_work;
-        k_scatter_batch<C, P, WEIGHT><<<grid, kBlock, 0, stream>>>(a, obs, n_obs, work_off,
-                                                                     n_work);
+        if (grid > n_work) grid = n_work;
+        if (grid > 0x7fffffffLL)
+            return set_error(SO3G_ERR_RANGE, "batch of %lld work items: too many blocks", grid);
+        k_scatter_batch<C, P, WEIGHT><<<(unsigned)grid, kBlock, 0, stream>>>(a, obs, n_obs,
+                                                                               work_off, n_work);
         return after_launch(WEIGHT ? "to_weight_map batch" : "to_map batch");
     }
 };

@@ -214,6 +214,31 @@ __device__ __forceinline__ long long hp_spread_bits(long long v) {
     return r;
 }
 
+// hpd2nest / hpd2ring (src/healpix_bare.c:109-114, 152-211): the pixel of
+// face f, in-face coordinates (ix, iy).
+__device__ __forceinline__ long long hp_hpd2pix(long long nside, bool nest, int f, long long ix,
+                                               long long iy) {
+    if (nest)  // hpd2nest
+        return (f * nside * nside) + hp_spread_bits(ix) + (hp_spread_bits(iy) << 1);
+    // hpd2ring
+    long long nl4 = 4 * nside;
+    long long jr = (hp_jrll(f) * nside) - ix - iy - 1;
+    if (jr < nside) {
+        long long jp = (hp_jpll(f) * jr + ix - iy + 1) / 2;
+        jp = (jp > nl4) ? jp - nl4 : ((jp < 1) ? jp + nl4 : jp);
+        return 2 * jr * (jr - 1) + jp - 1;
+    } else if (jr > 3 * nside) {
+        jr = nl4 - jr;
+        long long jp = (hp_jpll(f) * jr + ix - iy + 1) / 2;
+        jp = (jp > nl4) ? jp - nl4 : ((jp < 1) ? jp + nl4 : jp);
+        return 12 * nside * nside - 2 * (jr + 1) * jr + jp - 1;
+    } else {
+        long long jp = (hp_jpll(f) * nside + ix - iy + 1 + ((jr - nside) & 1)) / 2;
+        jp = (jp > nl4) ? jp - nl4 : ((jp < 1) ? jp + nl4 : jp);
+        return 2 * nside * (nside - 1) + (jr - nside) * nl4 + jp - 1;
+    }
+}
+
 // Returns the pixel, or -1 for a NaN/inf angle (the reference converts NaN
 // to an integer there, which is undefined).
 __device__ __forceinline__ long long hp_ang2pix(long long nside, bool nest, double theta,
@@ -257,25 +282,7 @@ __device__ __forceinline__ long long hp_ang2pix(long long nside, bool nest, doub
     }
     // loc2hpd
     long long ix = (long long)(hx * nside), iy = (long long)(hy * nside);
-    if (nest)  // hpd2nest
-        return (f * nside * nside) + hp_spread_bits(ix) + (hp_spread_bits(iy) << 1);
-    // hpd2ring
-    long long nl4 = 4 * nside;
-    long long jr = (hp_jrll(f) * nside) - ix - iy - 1;
-    if (jr < nside) {
-        long long jp = (hp_jpll(f) * jr + ix - iy + 1) / 2;
-        jp = (jp > nl4) ? jp - nl4 : ((jp < 1) ? jp + nl4 : jp);
-        return 2 * jr * (jr - 1) + jp - 1;
-    } else if (jr > 3 * nside) {
-        jr = nl4 - jr;
-        long long jp = (hp_jpll(f) * jr + ix - iy + 1) / 2;
-        jp = (jp > nl4) ? jp - nl4 : ((jp < 1) ? jp + nl4 : jp);
-        return 12 * nside * nside - 2 * (jr + 1) * jr + jp - 1;
-    } else {
-        long long jp = (hp_jpll(f) * nside + ix - iy + 1 + ((jr - nside) & 1)) / 2;
-        jp = (jp > nl4) ? jp - nl4 : ((jp < 1) ? jp + nl4 : jp);
-        return 2 * nside * (nside - 1) + (jr - nside) * nl4 + jp - 1;
-    }
+    return hp_hpd2pix(nside, nest, f, ix, iy);
 }
 
 // ---------------------------------------------------------------------------
@@ -516,6 +523,11 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
     e = (a - (s - bb)) + (b - bb);
 }
 
+// A warp with at least this many runs adds its terms with one atomic each:
+// its atomics already spread over many addresses, and the reduction would
+// cost more issue slots than the atomics it saves.
+constexpr int kDirectRuns = 4;
+
 // Sums the values of each run of equal keys across the warp (lanes in
 // order) and adds the run totals to map[key + mult[k] * plane] from the
 // run's first lane.  Keys < 0 are not flushed.  All 32 lanes must call.
@@ -526,6 +538,14 @@ __device__ __forceinline__ void flush_runs(long long key, long long plane, float
     long long prev = __shfl_up_sync(kFull, key, 1);
     bool head = (lane == 0) || (key != prev);
     unsigned heads = __ballot_sync(kFull, head);
+    if (__popc(heads) >= kDirectRuns) {
+        if (key >= 0) {
+#pragma unroll
+            for (int k = 0; k < NV; k++)
+                if ((vmask >> k) & 1u) atomicAdd(map + key + mult[k] * plane, f2d(v[k]));
+        }
+        return;
+    }
     unsigned after = heads & ~((2u << lane) - 1u);
     int end = after ? (__ffs(after) - 1) : 32;
     int span = head ? end - lane : 1;

@@ -1,5 +1,6 @@
-// fastpoint.cuh -- certified fast pointing for CAR with nearest-neighbour
-// flat pixelizors.
+// fastpoint.cuh -- certified fast pointing for the flat pixelizors
+// (nearest neighbour and bilinear, NonTiled and Tiled) of the CAR, TAN, ZEA
+// and SIN projections.
 //
 // GB300 executes float64 at 1/64 of the float32 rate, and the exact float64
 // pointing (quaternion compose, two table lookups, seven IEEE divisions, one
@@ -162,6 +163,7 @@ __device__ __forceinline__ float half_gap(float v) {
 struct FastTables {
     const float4 *asin_t;
     const float4 *atan2_t;
+    const float4 *asin_sc;   // (sin hi, sin lo, cos hi, cos lo) of the asin knots
 };
 
 // Piecewise-linear interpolant of a table at u in [0, 1]: the value of
@@ -179,43 +181,43 @@ struct FastConst {
     dfl inv_cdx, inv_cdy;   // 1/cdelt
     dfl off_x, off_y;       // crpix - 1 + 0.5
     dfl pi, half_pi;
+    dfl inv_2pi, third;     // the float64 constants 1/(2 pi) and 1/3
+    dfl two_thirds;         // the float64 constant 2/3
 };
 
-// The certified CAR pointing of one sample.  Returns false when the sample
-// must go to the exact path.  On success: *on_map, pix (flat nearest-
-// neighbour tuple as get_pixels<P> would give) and pf[0..2].
-template <int P>
-__device__ __forceinline__ bool fast_car(const DGeom &g, const FastTables &ft,
-                                         const FastConst &fc, const dfl (&qb)[4],
-                                         const dfl (&qd)[4], int nc, float T, float Pr,
-                                         int *pix, bool *on_map, float *pf) {
-    // q = qb * qd (Hamilton product).
-    const dfl a = df_dot<4>({qb[0], qb[1], qb[2], qb[3]},
-                            {qd[0], df_neg(qd[1]), df_neg(qd[2]), df_neg(qd[3])});
-    const dfl b = df_dot<4>({qb[0], qb[1], qb[2], qb[3]},
-                            {qd[1], qd[0], qd[3], df_neg(qd[2])});
-    const dfl c = df_dot<4>({qb[0], qb[1], qb[2], qb[3]},
-                            {qd[2], df_neg(qd[3]), qd[0], qd[1]});
-    const dfl d = df_dot<4>({qb[0], qb[1], qb[2], qb[3]},
-                            {qd[3], qd[2], df_neg(qd[1]), qd[0]});
-    // cos(theta) = a^2 - b^2 - c^2 + d^2 = sin(lat).
-    const dfl cos_t = df_dot<4>({a, b, c, d}, {a, df_neg(b), df_neg(c), d});
-    // Near the native poles (|lat| > ~87 deg) the tables' ends and the spin
-    // factors are ill-conditioned: exact path.
-    if (!(fabsf(cos_t.hi) < 0.998f)) return false;
-    // lat = ASIN(cos_t) (odd, continuous at 0).
-    const bool south = cos_t.hi < 0.f;
-    dfl lat = lut_df(ft.asin_t, south ? df_neg(cos_t) : cos_t);
-    if (south) lat = df_neg(lat);
-    // lon = ATAN2(c*d - a*b, c*a + d*b).
+// Native-frame quantities of one sample, in double-float, from the
+// boresight and detector quaternions (Pointer<C>::GetCoords,
+// src/Projection.cxx:372-437, 479-507, 337-364):
+//   X, Y    the coordinates the flat pixelizor divides by cdelt (CAR: lon,
+//           lat; zenithal: the projection-plane coordinates);
+//   Nc, Ns, D  with coords[2] = Nc / sqrt(D) and coords[3] = Ns / sqrt(D).
+// Returns false where the sample must take the exact path: the CAR
+// native poles and atan2 seam, and the zenithal projections far from their
+// pole (where the reference's expressions lose conditioning).
+// q = qb * qd (Hamilton product).
+__device__ __forceinline__ void df_qmul(const dfl (&qb)[4], const dfl (&qd)[4], dfl &a, dfl &b,
+                                        dfl &c, dfl &d) {
+    a = df_dot<4>({qb[0], qb[1], qb[2], qb[3]},
+                  {qd[0], df_neg(qd[1]), df_neg(qd[2]), df_neg(qd[3])});
+    b = df_dot<4>({qb[0], qb[1], qb[2], qb[3]}, {qd[1], qd[0], qd[3], df_neg(qd[2])});
+    c = df_dot<4>({qb[0], qb[1], qb[2], qb[3]}, {qd[2], df_neg(qd[3]), qd[0], qd[1]});
+    d = df_dot<4>({qb[0], qb[1], qb[2], qb[3]}, {qd[3], qd[2], df_neg(qd[1]), qd[0]});
+}
+
+// CAR longitude and the spin quantities (Pointer<ProjCAR>::GetCoords,
+// :479-507): lon = ATAN2(c*d - a*b, c*a + d*b); c = Nc/h, s = Ns/h with
+// h^2 = (1 - cos^2)/4 = D.  False at the +-pi seam (Y ~ 0 with X < 0),
+// a discontinuity of atan2.
+__device__ __forceinline__ bool fast_lon_spin(const FastTables &ft, const FastConst &fc,
+                                              const dfl &a, const dfl &b, const dfl &c,
+                                              const dfl &d, const dfl &cos_t, dfl &lon, dfl &Nc,
+                                              dfl &Ns, dfl &D) {
     const dfl cd = df_mul(c, d), ab = df_mul(a, b);
-    const dfl Y = df_sub(cd, ab);
-    const dfl X = df_dot<2>({c, d}, {a, b});
-    // The +-pi seam (Y ~ 0 with X < 0) is a discontinuity of atan2.
-    if (X.hi < 0.f && !(fabsf(Y.hi) > 1e-6f)) return false;
-    const bool neg = Y.hi < 0.f, mirror = X.hi < 0.f;
-    const dfl ay = neg ? df_neg(Y) : Y, ax = mirror ? df_neg(X) : X;
-    dfl lon;
+    const dfl Yv = df_sub(cd, ab);
+    const dfl Xv = df_dot<2>({c, d}, {a, b});
+    if (Xv.hi < 0.f && !(fabsf(Yv.hi) > 1e-6f)) return false;
+    const bool neg = Yv.hi < 0.f, mirror = Xv.hi < 0.f;
+    const dfl ay = neg ? df_neg(Yv) : Yv, ax = mirror ? df_neg(Xv) : Xv;
     if (ax.hi < ay.hi) {
         lon = df_sub(fc.half_pi, lut_df(ft.atan2_t, df_mul(ax, df_recip(ay))));
     } else {
@@ -223,10 +225,87 @@ __device__ __forceinline__ bool fast_car(const DGeom &g, const FastTables &ft,
     }
     if (mirror) lon = df_sub(fc.pi, lon);
     if (neg) lon = df_neg(lon);
+    // Spin (:1180-1209).
+    Nc = df_dot<2>({a, b}, {c, df_neg(d)});
+    Ns = df_add(cd, ab);
+    D = df_mulf(df_sub(dfl{1.f, 0.f}, df_mul(cos_t, cos_t)), 0.25f);
+    return true;
+}
 
-    // Pixel: x = lon / cdx + crpix_x - 1 + 0.5 (and y), integer part.
-    const dfl x = df_add(df_mul(lon, fc.inv_cdx), fc.off_x);
-    const dfl y = df_add(df_mul(lat, fc.inv_cdy), fc.off_y);
+template <int C>
+__device__ __forceinline__ bool fast_native(const FastTables &ft, const FastConst &fc,
+                                            const dfl (&qb)[4], const dfl (&qd)[4], dfl &X,
+                                            dfl &Y, dfl &Nc, dfl &Ns, dfl &D) {
+    dfl a, b, c, d;
+    df_qmul(qb, qd, a, b, c, d);
+    if (C == SO3G_COORD_CAR) {
+        // cos(theta) = a^2 - b^2 - c^2 + d^2 = sin(lat).
+        const dfl cos_t = df_dot<4>({a, b, c, d}, {a, df_neg(b), df_neg(c), d});
+        // Near the native poles (|lat| > ~87 deg) the tables' ends and the
+        // spin factors are ill-conditioned: exact path.
+        if (!(fabsf(cos_t.hi) < 0.998f)) return false;
+        // lat = ASIN(cos_t) (odd, continuous at 0).
+        const bool south = cos_t.hi < 0.f;
+        dfl lat = lut_df(ft.asin_t, south ? df_neg(cos_t) : cos_t);
+        if (south) lat = df_neg(lat);
+        Y = lat;
+        return fast_lon_spin(ft, fc, a, b, c, d, cos_t, X, Nc, Ns, D);
+    } else {
+        // Zenithal: cos^2(theta/2) = a^2 + d^2; coords[2] = (a^2 - d^2)/n,
+        // coords[3] = 2ad/n.
+        const dfl n = df_dot<2>({a, d}, {a, d});
+        const dfl u = df_dot<2>({a, c}, {b, df_neg(d)});   // a*b - c*d
+        const dfl v = df_dot<2>({a, b}, {c, d});           // a*c + b*d
+        if (C == SO3G_COORD_TAN) {
+            // :372-400: X = 2u / cos(theta), cos(theta) = 2n - 1.
+            const dfl ct = df_sub(df_mulf(n, 2.f), dfl{1.f, 0.f});
+            if (!(ct.hi > 1e-2f)) return false;
+            const dfl r = df_mulf(df_recip(ct), 2.f);
+            X = df_mul(u, r);
+            Y = df_mul(v, r);
+        } else if (C == SO3G_COORD_ZEA) {
+            // :408-437: X = 2u / sqrt(n).
+            if (!(n.hi > 1e-4f)) return false;
+            const float s0 = sqrtf(n.hi);
+            const float res = fmaf(-s0, s0, n.hi) + n.lo;   // n - s0^2
+            const dfl sq = fast_two_sum(s0, res / (2.f * s0));
+            const dfl r = df_mulf(df_recip(sq), 2.f);
+            X = df_mul(u, r);
+            Y = df_mul(v, r);
+        } else {
+            // SIN, :337-364: X = 2u, Y = 2v.
+            if (!(n.hi > 1e-4f)) return false;
+            X = df_mulf(u, 2.f);
+            Y = df_mulf(v, 2.f);
+        }
+        Nc = df_dot<2>({a, d}, {a, df_neg(d)});
+        Ns = df_mulf(df_mul(a, d), 2.f);
+        D = df_mul(n, n);
+        return true;
+    }
+}
+
+// Certified flat pixelization (Pixelizor2_Flat<NonTiled|Tiled, NN|Bilinear>
+// ::GetPixels, :912-952, :1124-1166) of the pixel coordinates x = X/cdx +
+// crx - 1 + 0.5 and y.  Returns false when an integer part is not certain.
+// Nearest neighbour: one tap of weight 1 on the map.  Bilinear: the taps
+// of the reference (same pixels, same order); each weight is the float32
+// nearest to the double-float value of the reference's weight, which is
+// the reference's float32 weight or one of its neighbours.
+template <int P>
+__device__ __forceinline__ bool fast_pixels(const DGeom &g, dfl x, dfl y, int (*pix)[3],
+                                            float *w, int &n) {
+    n = 0;
+    if (P == PX_FLAT_NT_BL || P == PX_FLAT_T_BL) {
+        // Far outside the map there is no tap (as in get_pixels).
+        if (!(x.hi > -4.f && x.hi < (float)g.nx + 4.f && y.hi > -4.f &&
+              y.hi < (float)g.ny + 4.f))
+            return x.hi == x.hi && y.hi == y.hi;
+    } else {
+        if (!(x.hi > -2.f && x.hi < (float)g.nx + 1.f && y.hi > -2.f &&
+              y.hi < (float)g.ny + 1.f))
+            return x.hi == x.hi && y.hi == y.hi;
+    }
     dfl fx, fy;
     const int ix = df_floor(x, fx), iy = df_floor(y, fy);
     if (!(fx.hi > kEpsPix && fx.hi < 1.f - kEpsPix && fy.hi > kEpsPix &&
@@ -234,33 +313,75 @@ __device__ __forceinline__ bool fast_car(const DGeom &g, const FastTables &ft,
         return false;
     if (P == PX_FLAT_NT_NN) {
         // :912-926 (x not near an integer: floor decides the bounds)
-        *on_map = ix >= 0 && ix < g.nx && iy >= 0 && iy < g.ny;
-        if (*on_map) {
-            pix[0] = iy;
-            pix[1] = ix;
+        if (ix >= 0 && ix < g.nx && iy >= 0 && iy < g.ny) {
+            pix[0][0] = iy;
+            pix[0][1] = ix;
+            w[0] = 1.f;
+            n = 1;
         }
-    } else {
+    } else if (P == PX_FLAT_T_NN) {
         // :1124-1138 (int() truncation: x in (-1, 0) lands in column 0)
         const int tx = (x.hi < 0.f) ? ix + 1 : ix, ty = (y.hi < 0.f) ? iy + 1 : iy;
-        *on_map = tx >= 0 && tx < g.nx && ty >= 0 && ty < g.ny && x.hi > -1.f && y.hi > -1.f;
-        if (*on_map) {
+        if (tx >= 0 && tx < g.nx && ty >= 0 && ty < g.ny) {
             const int sub_y = ty / g.ty, sub_x = tx / g.tx;
-            pix[0] = sub_y * g.ntx + sub_x;
-            pix[1] = ty - sub_y * g.ty;
-            pix[2] = tx - sub_x * g.tx;
+            pix[0][0] = sub_y * g.ntx + sub_x;
+            pix[0][1] = ty - sub_y * g.ty;
+            pix[0][2] = tx - sub_x * g.tx;
+            w[0] = 1.f;
+            n = 1;
+        }
+    } else {
+        // :930-952 (floor) and :1141-1166 (int() truncation, where x1 = ix + 1
+        // for negative x and the weight x - x1 is negative).
+        int x1 = ix, y1 = iy;
+        dfl wx0 = fx, wy0 = fy;
+        if (P == PX_FLAT_T_BL) {
+            if (x.hi < 0.f) {
+                x1 = ix + 1;
+                wx0 = df_sub(fx, dfl{1.f, 0.f});
+            }
+            if (y.hi < 0.f) {
+                y1 = iy + 1;
+                wy0 = df_sub(fy, dfl{1.f, 0.f});
+            }
+        }
+        const dfl wx[2] = {wx0, df_sub(dfl{1.f, 0.f}, wx0)};
+        const dfl wy[2] = {wy0, df_sub(dfl{1.f, 0.f}, wy0)};
+#pragma unroll
+        for (int dy = 0; dy < 2; dy++) {
+            const int yy = y1 + dy;
+            if (yy < 0 || yy >= g.ny) continue;
+#pragma unroll
+            for (int dx = 0; dx < 2; dx++) {
+                const int xx = x1 + dx;
+                if (xx < 0 || xx >= g.nx) continue;
+                if (P == PX_FLAT_NT_BL) {
+                    pix[n][0] = yy;
+                    pix[n][1] = xx;
+                } else {
+                    const int sub_y = yy / g.ty, sub_x = xx / g.tx;
+                    pix[n][0] = sub_y * g.ntx + sub_x;
+                    pix[n][1] = yy - sub_y * g.ty;
+                    pix[n][2] = xx - sub_x * g.tx;
+                }
+                w[n] = df_mul(wy[dy], wx[dx]).hi;
+                n++;
+            }
         }
     }
+    return true;
+}
 
-    // Spin factors (:1180-1209): c = Nc/h, s = Ns/h with h^2 = (1-cos^2)/4,
-    // so c*c - s*s = (Nc^2 - Ns^2)/D and 2*c*s = 2 Nc Ns / D, D = h^2.
+// Certified spin factors (spin_proj_factors, :1180-1209): float(P * (c*c -
+// s*s)) and float(P * 2*c*s) with c*c - s*s = (Nc^2 - Ns^2)/D and 2*c*s =
+// 2 Nc Ns / D.  Returns false when a float32 rounding is not certain.
+__device__ __forceinline__ bool fast_spin(int nc, float T, float Pr, const dfl &Nc,
+                                          const dfl &Ns, const dfl &D, float *pf) {
     if (nc == 1) {
         pf[0] = T;
         pf[1] = pf[2] = 0.f;
         return true;
     }
-    const dfl Nc = df_dot<2>({a, b}, {c, df_neg(d)});
-    const dfl Ns = df_add(cd, ab);
-    const dfl D = df_mulf(df_sub(dfl{1.f, 0.f}, df_mul(cos_t, cos_t)), 0.25f);
     const dfl invD = df_recip(D);
     const dfl v1 = df_mulf(df_mul(df_dot<2>({Nc, Ns}, {Nc, df_neg(Ns)}), invD), Pr);
     const dfl v2 = df_mulf(df_mul(df_mulf(df_mul(Nc, Ns), 2.f), invD), Pr);
@@ -281,6 +402,147 @@ __device__ __forceinline__ bool fast_car(const DGeom &g, const FastTables &ft,
         pf[2] = v2.hi;
     }
     return true;
+}
+
+// Integer part of a double-float whose fraction is certified to be at
+// least e from 0 and 1; false otherwise.
+__device__ __forceinline__ bool df_floor_cert(dfl x, float e, int &i) {
+    dfl f;
+    i = df_floor(x, f);
+    return f.hi > e && f.hi < 1.f - e;
+}
+
+// Certified HEALPix pixel (Pixelizor_Healpix::GetPixels, :565-574 and
+// :713-724, through ang2pix of src/healpix_bare.c:46-78, 271-306) of a
+// sample with sin(lat) = cos_t and longitude lon.  The reference forms
+// theta = pi/2 - lat from the table value of lat and takes its sin and cos
+// with the math library; here sin/cos(lat) come from the tabulated sin/cos
+// of the asin knot below lat and the series of the remaining angle
+// (|delta| < 1e-3 for |cos_t| < 0.998).  Every integer decision of ang2pix
+// (the equatorial/polar split, the wrap of phi, the face, the in-face
+// indices) is certified with a margin far above the double-float error;
+// false sends the sample to the exact path.  Off-map cannot happen.
+template <int P>
+__device__ __forceinline__ bool fast_healpix(const DGeom &g, const FastTables &ft,
+                                             const FastConst &fc, const dfl &cos_t,
+                                             const dfl &lon, int (*pix)[3], int &n) {
+    const long long nside = g.nside;
+    if (nside > (1LL << 20)) return false;   // in-face indices beyond float's integers
+    // lat = v_i + delta (the table's knot and the interpolated remainder).
+    const bool south = cos_t.hi < 0.f;
+    const dfl u = south ? df_neg(cos_t) : cos_t;
+    dfl frac;
+    int i = df_floor(df_mulf(u, (float)(kLutN - 1)), frac);
+    i = max(0, min(i, kLutN - 2));
+    const float4 k = __ldg(ft.asin_t + i);
+    const float4 sc = __ldg(ft.asin_sc + i);
+    const dfl delta = df_mul(dfl{k.z, k.w}, frac);
+    const dfl d2 = df_mul(delta, delta);
+    const float d3 = delta.hi * d2.hi;
+    const dfl sin_d = df_add(delta, dfl{d3 * (-1.f / 6.f), 0.f});
+    const dfl cos_d = df_add(dfl{1.f, 0.f},
+                             df_add(df_mulf(d2, -0.5f), dfl{d2.hi * d2.hi * (1.f / 24.f), 0.f}));
+    const dfl S = dfl{sc.x, sc.y}, Cc = dfl{sc.z, sc.w};
+    dfl z = df_add(df_mul(S, cos_d), df_mul(Cc, sin_d));     // sin(lat) = cos(theta)
+    const dfl s = df_sub(df_mul(Cc, cos_d), df_mul(S, sin_d)); // cos(lat) = sin(theta)
+    if (south) z = df_neg(z);
+    // The float64 roundings of the reference (theta, sincos) move z and s by
+    // ~1e-16; the double-float error is below 1e-12.
+    const float ez = 1e-11f;
+    const float e = fmaxf(kEpsPix, 1e-10f * (float)nside);
+    const dfl za = z.hi < 0.f ? df_neg(z) : z;
+    // x = phi / (2 pi) wrapped into [0, 1); tt = 4 x.
+    dfl x = df_mul(lon, fc.inv_2pi);
+    if (!(fabsf(x.hi) > ez)) return false;
+    if (x.hi < 0.f) x = df_add(x, dfl{1.f, 0.f});
+    const dfl tt = df_mulf(x, 4.f);
+    const float fn = (float)nside;
+    int f, ix, iy;
+    // za <= 2/3, against the float64 constant 2/3 (a float comparison would
+    // misplace the boundary by the float rounding of 2/3).
+    const dfl dz = df_sub(za, fc.two_thirds);
+    if (!(fabsf(dz.hi) > ez)) return false;
+    if (dz.hi < 0.f) {
+        // Equatorial belt (za <= 2/3; |za - 2/3| certified above).
+        const dfl t1 = df_add(dfl{0.5f, 0.f}, tt);
+        const dfl t2 = df_mulf(z, 0.75f);
+        const dfl jp = df_sub(t1, t2), jm = df_add(t1, t2);
+        int Jp, Jm;
+        if (!df_floor_cert(df_mulf(jp, fn), e, Jp)) return false;
+        if (!df_floor_cert(df_mulf(jm, fn), e, Jm)) return false;
+        // jp*nside and jm*nside are not integers, so floor(jp) is
+        // floor(jp*nside) div nside (jp, jm >= 0).
+        if (Jp < 0 || Jm < 0) return false;
+        const int ifp = Jp / (int)nside, ifm = Jm / (int)nside;
+        // hx = jm - ifm, hy = 1 + ifp - jp.
+        ix = Jm - ifm * (int)nside;
+        iy = (1 + ifp) * (int)nside - Jp - 1;
+        f = (ifp == ifm) ? (ifp | 4) : ((ifp < ifm) ? ifp : (ifm + 8));
+    } else {
+        // Polar caps.
+        int ntt;
+        if (!df_floor_cert(tt, ez, ntt)) return false;
+        if (ntt >= 4) ntt = 3;
+        const dfl tp = df_sub(tt, dfl{(float)ntt, 0.f});
+        // tmp = s / sqrt((1 + za) * (1/3)).
+        const dfl q = df_mul(df_add(dfl{1.f, 0.f}, za), fc.third);
+        const float r0 = sqrtf(q.hi);
+        const dfl sq = fast_two_sum(r0, (fmaf(-r0, r0, q.hi) + q.lo) / (2.f * r0));
+        const dfl tmp = df_mul(s, df_recip(sq));
+        const dfl jp = df_mul(tp, tmp), jm = df_mul(df_sub(dfl{1.f, 0.f}, tp), tmp);
+        // The clamps at 1 only act within rounding of za = 2/3.
+        if (!(jp.hi < 1.f - ez && jm.hi < 1.f - ez)) return false;
+        dfl hx, hy;
+        if (z.hi >= 0.f) {
+            hx = df_sub(dfl{1.f, 0.f}, jm);
+            hy = df_sub(dfl{1.f, 0.f}, jp);
+            f = ntt;
+        } else {
+            hx = jp;
+            hy = jm;
+            f = ntt + 8;
+        }
+        if (!df_floor_cert(df_mulf(hx, fn), e, ix)) return false;
+        if (!df_floor_cert(df_mulf(hy, fn), e, iy)) return false;
+    }
+    const long long ip = hp_hpd2pix(nside, P == PX_HP_T ? true : (g.nest != 0), f, ix, iy);
+    if (ip < 0 || ip >= g.npix) return false;
+    if (P == PX_HP_NT) {
+        pix[0][0] = (int)ip;
+    } else {
+        pix[0][0] = (int)(ip / g.nppt);
+        pix[0][1] = (int)(ip % g.nppt);
+    }
+    n = 1;
+    return true;
+}
+
+// The certified pointing of one sample: taps (pixels, weights) and spin
+// factors equal to the exact path's (bilinear weights: see fast_pixels).
+// Returns false when the sample must go to the exact path.
+template <int C, int P>
+__device__ __forceinline__ bool fast_pointing(const DGeom &g, const FastTables &ft,
+                                              const FastConst &fc, const dfl (&qb)[4],
+                                              const dfl (&qd)[4], int nc, float T, float Pr,
+                                              int (*pix)[3], float *w, int &n, float *pf) {
+    if (P == PX_HP_NT || P == PX_HP_T) {
+        dfl a, b, c, d;
+        df_qmul(qb, qd, a, b, c, d);
+        const dfl cos_t = df_dot<4>({a, b, c, d}, {a, df_neg(b), df_neg(c), d});
+        if (!(fabsf(cos_t.hi) < 0.998f)) return false;
+        dfl lon, Nc, Ns, D;
+        if (!fast_lon_spin(ft, fc, a, b, c, d, cos_t, lon, Nc, Ns, D)) return false;
+        if (!fast_healpix<P>(g, ft, fc, cos_t, lon, pix, n)) return false;
+        w[0] = 1.f;
+        return fast_spin(nc, T, Pr, Nc, Ns, D, pf);
+    }
+    dfl X, Y, Nc, Ns, D;
+    if (!fast_native<C>(ft, fc, qb, qd, X, Y, Nc, Ns, D)) return false;
+    const dfl x = df_add(df_mul(X, fc.inv_cdx), fc.off_x);
+    const dfl y = df_add(df_mul(Y, fc.inv_cdy), fc.off_y);
+    if (!fast_pixels<P>(g, x, y, pix, w, n)) return false;
+    if (n == 0) return true;   // off the map: nothing to add
+    return fast_spin(nc, T, Pr, Nc, Ns, D, pf);
 }
 
 // sig + m * pf rounded to float32 as the reference's `*sig += map * pf`
@@ -305,6 +567,34 @@ __device__ __forceinline__ bool fast_accum(float &sig, double m, float pf) {
     // Error: double-float ~2^-46 and the reference's two float64 roundings,
     // relative to the operands.
     const float e = 5e-13f * (fabsf(p) + fabsf(sig));
+    if (!(fabsf(s.hi) > 1e-30f && fabsf(s.lo) + e < half_gap(s.hi))) return false;
+    sig = s.hi;
+    return true;
+}
+
+// The same for a bilinear tap: sig + m * pf * w as the reference's
+// `*sig += map * pf * w` (two float64 products, a float64 sum, then
+// float32).
+__device__ __forceinline__ bool fast_accum(float &sig, double m, float pf, float w) {
+    if (w == 1.f) return fast_accum(sig, m, pf);
+    const int mh = __double2hiint(m);
+    if ((((unsigned)mh & 0x7fffffffu) | (unsigned)__double2loint(m)) == 0u || pf == 0.f ||
+        w == 0.f) {
+        sig = sig + __int_as_float((mh ^ __float_as_int(pf) ^ __float_as_int(w)) & 0x80000000);
+        return true;
+    }
+    dfl md;
+    if (!df_split(m, md)) return false;
+    const float p0 = md.hi * pf;
+    float pe = fmaf(md.hi, pf, -p0);
+    pe = fmaf(md.lo, pf, pe);
+    const dfl t = df_mulf(fast_two_sum(p0, pe), w);
+    dfl s = two_sum(sig, t.hi);
+    s.lo += t.lo;
+    s = fast_two_sum(s.hi, s.lo);
+    // Error: double-float ~2^-45 and the reference's three float64
+    // roundings, relative to the operands.
+    const float e = 5e-13f * (fabsf(t.hi) + fabsf(sig));
     if (!(fabsf(s.hi) > 1e-30f && fabsf(s.lo) + e < half_gap(s.hi))) return false;
     sig = s.hi;
     return true;

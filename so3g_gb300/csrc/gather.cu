@@ -2,8 +2,8 @@
 // accumulated into the float32 signal exactly as the reference does (each
 // term added in float64 and rounded to float32).
 //
-// CAR with a nearest-neighbour flat pixelizor uses the certified
-// double-float pointing of fastpoint.cuh (when GatherArgs::fast is set);
+// CAR, TAN, ZEA and SIN with flat pixelizors use the certified double-float
+// pointing of fastpoint.cuh (when GatherArgs::fast is set);
 // samples it cannot certify are queued in shared memory and finished by the
 // exact float64 pointing, so every sample's result equals the exact path's.
 
@@ -69,9 +69,14 @@ __device__ void exact_gather(const GatherArgs &a, int det, int t, const QuatD &o
 }
 
 template <int C, int P>
-__global__ void __launch_bounds__(kBlock) k_from_map(GatherArgs a) {
+// Compiled for 5 resident blocks per SM (at most 51 registers).
+__global__ void __launch_bounds__(kBlock, 5) k_from_map(GatherArgs a) {
     constexpr bool kFastOK =
-        C == SO3G_COORD_CAR && (P == PX_FLAT_NT_NN || P == PX_FLAT_T_NN);
+        (C == SO3G_COORD_CAR || C == SO3G_COORD_TAN || C == SO3G_COORD_ZEA ||
+         C == SO3G_COORD_SIN) &&
+        (P == PX_FLAT_NT_NN || P == PX_FLAT_T_NN || P == PX_FLAT_NT_BL ||
+         P == PX_FLAT_T_BL) ||
+        (C == SO3G_COORD_CAR && (P == PX_HP_NT || P == PX_HP_T));
     __shared__ int s_queue[kFastOK ? kQueueCap : 1];
     __shared__ int s_qn;
     int det, t0, t1;
@@ -99,24 +104,29 @@ __global__ void __launch_bounds__(kBlock) k_from_map(GatherArgs a) {
             bool ok = df_split(lo.x, qb[0]) & df_split(lo.y, qb[1]) & df_split(hi.x, qb[2]) &
                       df_split(hi.y, qb[3]);
             int pix[NT][3];
-            float pf[3];
-            bool on = false;
-            ok = ok && fast_car<P>(a.g, a.ft, a.fc, qb, qd, nc, T, Pr, pix[0], &on, pf);
-            if (ok && on) {
-                long long off, plane;
-                const int bad = locate<P>(a.g, pix[0], &off, &plane);
-                if (bad >= 0) {
-                    record_missing_tile(a.err, bad);
-                } else {
-                    // src/Projection.cxx:1763-1765 with certified float32
-                    // roundings (nearest neighbour: weight 1).
-                    float *sp = a.signal + det * a.sig_stride + t;
-                    float s = *sp;
+            float pf[3], w[NT];
+            int n = 0;
+            ok = ok && fast_pointing<C, P>(a.g, a.ft, a.fc, qb, qd, nc, T, Pr, pix, w, n, pf);
+            if (ok && n > 0) {
+                // src/Projection.cxx:1763-1765 with certified float32
+                // roundings, tap by tap and component by component.
+                float *sp = a.signal + det * a.sig_stride + t;
+                float s = *sp;
+#pragma unroll
+                for (int k = 0; k < NT; k++) {
+                    if (k >= n || !ok) break;
+                    long long off, plane;
+                    const int bad = locate<P>(a.g, pix[k], &off, &plane);
+                    if (bad >= 0) {
+                        record_missing_tile(a.err, bad);
+                        continue;
+                    }
 #pragma unroll
                     for (int c = 0; c < 3; c++)
-                        if (ok && c < nc) ok = fast_accum(s, __ldg(a.map + off + c * plane), pf[c]);
-                    if (ok) *sp = s;
+                        if (ok && c < nc)
+                            ok = fast_accum(s, __ldg(a.map + off + c * plane), pf[c], w[k]);
                 }
+                if (ok) *sp = s;
             }
             if (!ok) s_queue[atomicAdd(&s_qn, 1)] = t;
         }

@@ -9,7 +9,7 @@
 // (compensated float32) and flushed with one float64 atomic per run and
 // component.  The ATOMIC accumulator adds every term on its own.
 //
-// Pointing: CAR with a nearest-neighbour flat pixelizor uses the certified
+// Pointing: CAR, TAN, ZEA and SIN with flat pixelizors use the certified
 // double-float pointing of fastpoint.cuh when ScatterArgs::fast is set;
 // samples it cannot certify are queued in shared memory and recomputed by
 // the exact float64 pointing, with plain atomics, when the queue fills and
@@ -26,6 +26,9 @@ namespace so3g {
 namespace {
 
 constexpr int kQueueCap = 512;
+// Resident blocks per SM the scatter kernels are compiled for (caps their
+// registers at 65536 / (kBlock * 5) = 51).
+constexpr int kScatterBlocksPerSM = 5;
 
 struct ScatterArgs {
     DGeom g;
@@ -48,7 +51,11 @@ struct ScatterArgs {
 template <int C, int P>
 struct FastEligible {
     static constexpr bool value =
-        C == SO3G_COORD_CAR && (P == PX_FLAT_NT_NN || P == PX_FLAT_T_NN);
+        (C == SO3G_COORD_CAR || C == SO3G_COORD_TAN || C == SO3G_COORD_ZEA ||
+         C == SO3G_COORD_SIN) &&
+        (P == PX_FLAT_NT_NN || P == PX_FLAT_T_NN || P == PX_FLAT_NT_BL ||
+         P == PX_FLAT_T_BL) ||
+        (C == SO3G_COORD_CAR && (P == PX_HP_NT || P == PX_HP_T));
 };
 
 // Value slots: to_map slot c = component c; to_weight_map slots are the
@@ -167,11 +174,8 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
                 dfl qb[4];
                 bool ok = df_split(lo.x, qb[0]) & df_split(lo.y, qb[1]) &
                           df_split(hi.x, qb[2]) & df_split(hi.y, qb[3]);
-                bool on = false;
-                if (ok && fast_car<P>(a.g, a.ft, a.fc, qb, qd, nc, T, Pr, pix[0], &on, pf)) {
-                    n = on ? 1 : 0;
-                    w[0] = 1.f;
-                } else {
+                if (!(ok && fast_pointing<C, P>(a.g, a.ft, a.fc, qb, qd, nc, T, Pr, pix, w, n,
+                                                pf))) {
                     s_queue[atomicAdd(&s_qn, 1)] = t;
                     n = 0;
                 }
@@ -225,7 +229,7 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
 }
 
 template <int C, int P, bool WEIGHT>
-__global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs a) {
+__global__ void __launch_bounds__(kBlock, kScatterBlocksPerSM) k_scatter(ScatterArgs a) {
     __shared__ int s_queue[FastEligible<C, P>::value ? kQueueCap : 1];
     __shared__ int s_qn;
     int det, t0, t1;

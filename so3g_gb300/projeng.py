@@ -383,6 +383,105 @@ class _DevRanges:
 
 
 # ---------------------------------------------------------------------------
+# Streaming of host signals.
+#
+# A signal held in host memory is moved through the device in chunks of
+# detector rows, double-buffered: while the kernel of one chunk runs, the
+# next chunk is copied in on one copy stream and the previous one copied
+# out on another.  The device then holds two chunk buffers instead of the
+# whole signal, and the copies overlap the kernels.
+
+STREAM_MIN_BYTES = 64 << 20      # smaller signals go through the device whole
+STREAM_CHUNK_BYTES = 128 << 20   # bytes of signal per chunk
+_copy_streams = {}
+
+
+def _streams():
+    dev = torch.cuda.current_device()
+    if dev not in _copy_streams:
+        _copy_streams[dev] = (torch.cuda.Stream(), torch.cuda.Stream())
+    return _copy_streams[dev]
+
+
+def _host_matrix(sig):
+    """The host (n_det, n_time) float32 matrix behind a _Signal argument if
+    it can be streamed (one contiguous host array, large enough), else
+    None."""
+    if sig.device_mode or sig.rows is not None or sig._create:
+        return None
+    a = sig._src
+    if isinstance(a, torch.Tensor):
+        if a.is_cuda or a.dim() != 2 or not a.is_contiguous():
+            return None
+        t = a
+    else:
+        if a.ndim != 2 or not a.flags.c_contiguous or not a.flags.writeable:
+            return None
+        t = torch.from_numpy(a)
+    return t if t.numel() * 4 >= STREAM_MIN_BYTES else None
+
+
+def _stream_rows(host, launch, upload, download):
+    """Runs launch(d0, d1, buf) over chunks [d0, d1) of the rows of `host`
+    (a CPU float32 (n_det, n_time) tensor), buf being a device copy of
+    host[d0:d1] (upload) or zeros, and copies buf back into host[d0:d1]
+    afterwards (download).  Returns when every copy is complete."""
+    n_det, n_time = host.shape
+    if n_det == 0 or n_time == 0:
+        return
+    dev = _device()
+    comp = torch.cuda.current_stream()
+    h2d, d2h = _streams()
+    pinned = host.is_pinned()
+    rows = max(1, min(n_det, STREAM_CHUNK_BYTES // max(1, 4 * n_time)))
+    bufs = [torch.empty((rows, n_time), dtype=torch.float32, device=dev) for _ in range(2)]
+    h2d.wait_stream(comp)
+    freed = [None, None]    # event: the buffer's last use (kernel, download) done
+    pending = None          # the chunk to copy out once the next one is launched
+
+    def copy_out(job):
+        k, d0, d1, buf, done = job
+        with torch.cuda.stream(d2h):
+            d2h.wait_event(done)
+            host[d0:d1].copy_(buf, non_blocking=pinned)
+            out = torch.cuda.Event()
+            out.record(d2h)
+        freed[k] = out
+
+    for i, d0 in enumerate(range(0, n_det, rows)):
+        d1 = min(n_det, d0 + rows)
+        k = i % 2
+        buf = bufs[k][:d1 - d0]
+        with torch.cuda.stream(h2d):
+            if freed[k] is not None:
+                h2d.wait_event(freed[k])
+            if upload:
+                buf.copy_(host[d0:d1], non_blocking=pinned)
+            else:
+                buf.zero_()
+            ready = torch.cuda.Event()
+            ready.record(h2d)
+        comp.wait_event(ready)
+        launch(d0, d1, buf)
+        done = torch.cuda.Event()
+        done.record(comp)
+        freed[k] = done
+        if pending is not None:
+            copy_out(pending)
+            pending = None
+        if download:
+            pending = (k, d0, d1, buf, done)
+    if pending is not None:
+        copy_out(pending)
+    for b in bufs:
+        b.record_stream(h2d)
+        b.record_stream(d2h)
+    comp.wait_stream(h2d)
+    comp.wait_stream(d2h)
+    comp.synchronize()
+
+
+# ---------------------------------------------------------------------------
 # Maps.
 
 class _MapArg:
@@ -764,11 +863,22 @@ class ProjEngBase:
         resp = as_array(response, "response", "float32", (n_det, 2))
         bore, dets, resp = self._up((bore, "float64"), (dets, "float64"), (resp, "float32"))
         m.upload()
-        sig.upload()
         err = _ErrRecord()
-        _abi.check(_abi.lib().so3g_proj_from_map(
-            self._pz(), bore.data_ptr(), n_time, dets.data_ptr(), n_det, resp.data_ptr(),
-            m.struct, sig.dev.data_ptr(), sig.det_stride, err.ptr, _stream()), "from_map")
+        lib, pz = _abi.lib(), self._pz()
+
+        def launch(d0, d1, buf):
+            _abi.check(lib.so3g_proj_from_map(
+                pz, bore.data_ptr(), n_time, dets.data_ptr() + 32 * d0, d1 - d0,
+                resp.data_ptr() + 8 * d0, m.struct, buf.data_ptr(), buf.stride(0), err.ptr,
+                _stream()), "from_map")
+
+        host = _host_matrix(sig)
+        if host is not None:
+            _stream_rows(host, launch, upload=True, download=True)
+            err.raise_if_set()
+            return sig.ret
+        sig.upload()
+        launch(0, n_det, sig.dev)
         err.raise_if_set()
         sig.writeback()
         return sig.ret
@@ -787,13 +897,26 @@ class ProjEngBase:
         bore, dets, resp, w = self._up((bore, "float64"), (dets, "float64"),
                                        (resp, "float32"), (w, "float32"))
         m.upload()
-        sig.upload()
-        rng.upload()
         err = _ErrRecord()
-        _abi.check(_abi.lib().so3g_proj_to_map(
-            self._pz(), bore.data_ptr(), n_time, dets.data_ptr(), n_det, resp.data_ptr(),
-            sig.dev.data_ptr(), sig.det_stride, _ptr(w), rng.ptr(), m.struct,
-            DEFAULT_ACCUM if accum is None else accum, err.ptr, _stream()), "to_map")
+        lib, pz = _abi.lib(), self._pz()
+        acc = DEFAULT_ACCUM if accum is None else accum
+        host = _host_matrix(sig) if rng.seg_host is None else None
+        if host is not None:
+            def launch(d0, d1, buf):
+                _abi.check(lib.so3g_proj_to_map(
+                    pz, bore.data_ptr(), n_time, dets.data_ptr() + 32 * d0, d1 - d0,
+                    resp.data_ptr() + 8 * d0, buf.data_ptr(), buf.stride(0),
+                    None if w is None else w.data_ptr() + 4 * d0, None, m.struct, acc,
+                    err.ptr, _stream()), "to_map")
+
+            _stream_rows(host, launch, upload=True, download=False)
+        else:
+            sig.upload()
+            rng.upload()
+            _abi.check(lib.so3g_proj_to_map(
+                pz, bore.data_ptr(), n_time, dets.data_ptr(), n_det, resp.data_ptr(),
+                sig.dev.data_ptr(), sig.det_stride, _ptr(w), rng.ptr(), m.struct, acc,
+                err.ptr, _stream()), "to_map")
         err.raise_if_set()
         m.writeback()
         return map

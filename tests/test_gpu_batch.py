@@ -91,12 +91,14 @@ def test_batch_matches_oracle(orc, gpulib, coord, tiled, bilinear, hp, piece):
         got = (b.to_weight_map(m, piece=piece) if weight else b.to_map(m, piece=piece))
         assert got is m
         scale = max(np.abs(flat).max(), 1.0)
-        assert np.abs(stack_map(m) - flat).max() <= 1e-12 * scale
+        # Certified bilinear weights are within one float32 ulp.
+        rtol = 1e-6 if bilinear else 1e-12
+        assert np.abs(stack_map(m) - flat).max() <= rtol * scale
         seq = _sequential(c.eng, obs, lead, c.blank, weight)
         assert np.abs(stack_map(seq) - stack_map(m)).max() <= 1e-12 * scale
 
 
-@pytest.mark.parametrize("blocks", [1, 3, 0, 4096])
+@pytest.mark.parametrize("blocks", [1, 3, 0, 4096, -1, -2])
 def test_batch_grid_sizes(orc, gpulib, blocks):
     """Any grid size covers every work item exactly once."""
     c = _case(orc, "CAR")
@@ -125,6 +127,14 @@ def test_batch_device_tensors_and_graph(orc, gpulib):
     w = torch.zeros_like(w1)
     g = b.graph(m, w)
     assert g.launches == 2
+    # The per-observation strategy in a graph gives the same sums.
+    m2 = torch.zeros_like(m1)
+    w2 = torch.zeros_like(w1)
+    g2 = b.graph(m2, w2, map_shape=(8192, -2), weight_shape=(8192, -2))
+    g2.replay()
+    torch.cuda.synchronize()
+    assert float((m2 - m1).abs().max()) <= 1e-12 * scale
+    assert float((w2 - w1).abs().max()) <= 1e-12 * float(w1.abs().max())
     for _ in range(3):
         g.replay()
     torch.cuda.synchronize()
@@ -148,8 +158,8 @@ def test_tuner_and_cache(orc, gpulib, tmp_path, monkeypatch):
     b = ObservationBatch(c.eng, obs)
     assert b.tuned() is None
     piece, blocks = b.tune(pieces=(256, 1024), blocks_per_sm=(0, 2), reps=1)
-    assert piece in (256, 1024)
-    assert len(b.tune_log) == 4
+    assert (piece, blocks) in [(r["piece"], r["blocks"]) for r in b.tune_log]
+    assert len(b.tune_log) == 5
     assert b.tuned() == (piece, blocks)
     d = json.loads(cache.read_text())
     assert len(d) == 1
