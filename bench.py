@@ -237,6 +237,15 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# DRAM bytes per sample (dram__bytes_read.sum + dram__bytes_write.sum / samples)
+# of one ncu capture of the certified to_map and from_map kernels, CAR TQU
+# 3x2000x2000, 200 det x 1M samples (profiles/to_map_from_map_certified_
+# car_tqu_200det_1M.md).  The traffic is the signal (4 B read, from_map also
+# 4 B written) plus the boresight per detector, so it scales with the samples.
+MEASURED_TRAFFIC_PER_SAMPLE = {"to_map": (834.33e6 + 3.78e6) / 2e8,
+                               "from_map": (835.40e6 + 747.14e6) / 2e8}
+
+
 def algorithmic_bytes(c, op):
     """Compulsory bytes per (det, sample) of an operation (map of
     3 x npix float64)."""
@@ -326,6 +335,7 @@ def run_ours(args, c, rank, world):
         e_end = torch.cuda.Event(enable_timing=True)
         per = {op: [] for op in ops}
         with ClockSampler(dev.index) as clk:
+            torch.cuda.nvtx.range_push("timed")
             e_start.record(stream)
             for _ in range(steps):
                 t = step(accum)
@@ -333,6 +343,7 @@ def run_ours(args, c, rank, world):
                     per[op].append(ev)
             e_end.record(stream)
             torch.cuda.synchronize()
+            torch.cuda.nvtx.range_pop()
         if world > 1:
             torch.distributed.barrier()
         launches = lib.so3g_launch_count() - n0
@@ -679,7 +690,10 @@ def main():
             "data": "synthetic", "config": cfg,
             "op_ms": res["op_ms"],
             "roofline": {"bound": "hbm", "kernel": op, "achieved": achieved, "peak": hbm,
-                         "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                         "unit": "GB/s", "frac": achieved / hbm,
+                         "traffic": (MEASURED_TRAFFIC_PER_SAMPLE[op] * N
+                                     if c["kind"] == "car" and op in MEASURED_TRAFFIC_PER_SAMPLE
+                                     else None),
                          "bytes_per_sample": B, "peak_kind": kind},
             "clocks": res["clocks"], "gpu_launches": int(res["launches"])}
     if "fp64_path" in res:

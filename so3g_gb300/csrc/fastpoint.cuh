@@ -168,11 +168,19 @@ struct FastTables {
 
 // Piecewise-linear interpolant of a table at u in [0, 1]: the value of
 // LookupTable::get_raw (include/so_linterp.h:20-29) up to float64 rounding.
+// The knot below u * (n-1) and the remaining fraction, with the knot
+// index kept in [0, n-2]: at u = 1 (the last knot, which get_raw returns
+// for d >= n-1) that is knot n-2 with fraction 1.
+__device__ __forceinline__ int lut_index(dfl u, dfl &frac) {
+    const int i = df_floor(df_mulf(u, (float)(kLutN - 1)), frac);
+    const int ic = max(0, min(i, kLutN - 2));
+    if (ic != i) frac = df_add(frac, dfl{(float)(i - ic), 0.f});
+    return ic;
+}
+
 __device__ __forceinline__ dfl lut_df(const float4 *t, dfl u) {
-    dfl d = df_mulf(u, (float)(kLutN - 1));
     dfl frac;
-    int i = df_floor(d, frac);
-    i = max(0, min(i, kLutN - 2));
+    const int i = lut_index(u, frac);
     float4 k = __ldg(t + i);
     return df_add(dfl{k.x, k.y}, df_mul(dfl{k.z, k.w}, frac));
 }
@@ -432,8 +440,7 @@ __device__ __forceinline__ bool fast_healpix(const DGeom &g, const FastTables &f
     const bool south = cos_t.hi < 0.f;
     const dfl u = south ? df_neg(cos_t) : cos_t;
     dfl frac;
-    int i = df_floor(df_mulf(u, (float)(kLutN - 1)), frac);
-    i = max(0, min(i, kLutN - 2));
+    const int i = lut_index(u, frac);
     const float4 k = __ldg(ft.asin_t + i);
     const float4 sc = __ldg(ft.asin_sc + i);
     const dfl delta = df_mul(dfl{k.z, k.w}, frac);

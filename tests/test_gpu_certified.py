@@ -388,3 +388,21 @@ def test_certified_healpix_edges(orc):
             out[mode] = [eng.from_map(m, qd, dd, rd, None).cpu().numpy() for m in maps]
         for a, b in zip(out[_abi.POINTING_EXACT], out[_abi.POINTING_CERTIFIED]):
             assert bits_equal(a, b)
+
+
+def test_certified_octant_boundaries():
+    """CAR samples with |Y| = |X| in the atan2 of the longitude (lon =
+    +-pi/4, +-3pi/4), where the table is read at its last knot."""
+    n = 20000
+    rng = np.random.default_rng(47)
+    lon = rng.choice([np.pi / 4, -np.pi / 4, 3 * np.pi / 4, -3 * np.pi / 4], n) + \
+        rng.choice([0., 1e-15, -1e-15, 1e-12], n)
+    lat = rng.uniform(-1.3, 1.3, n)
+    q = _quats_at(lon, lat, rng.uniform(0, np.pi, n))
+    dets = np.array([[1., 0., 0., 0.]])
+    resp = np.ones((1, 2), np.float32)
+    p, eng = _engine((200, 200), 60 * ARCMIN, False)
+    # 0.9 deg pixels over 360 deg x 180 deg, so that all four lons are on the map.
+    eng2 = type(eng)((200, 400, 0.9 * np.pi / 180, -0.9 * np.pi / 180, 100.5, 200.5))
+    res = _compare(eng2, q, dets, resp, False, 3)
+    assert (res[0] > 0).mean() > 0.9
