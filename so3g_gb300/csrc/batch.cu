@@ -17,8 +17,7 @@ template <int C, int P, bool WEIGHT>
 __global__ void __launch_bounds__(kBlock, kScatterBlocksPerSM)
     k_scatter_batch(ScatterArgs base, const so3g_obs *obs, int n_obs,
                     const long long *work_off, long long n_work) {
-    __shared__ int s_queue[FastEligible<C, P>::value ? kQueueCap : 1];
-    __shared__ int s_qn;
+    __shared__ int s_queue[FastEligible<C, P>::value ? (kBlock / 32) * kWarpQueue : 1];
     for (long long w = blockIdx.x; w < n_work; w += gridDim.x) {
         // The observation holding item w: largest o with work_off[o] <= w.
         int lo = 0, hi = n_obs - 1;
@@ -46,7 +45,7 @@ __global__ void __launch_bounds__(kBlock, kScatterBlocksPerSM)
         a.signal = ob.signal;
         a.sig_stride = ob.sig_det_stride;
         a.det_weights = ob.det_weights;
-        scatter_piece<C, P, WEIGHT>(a, det, t0, t1, s_queue, s_qn);
+        scatter_piece<C, P, WEIGHT>(a, det, t0, t1, s_queue);
     }
 }
 

@@ -35,6 +35,21 @@
 
 namespace so3g {
 
+// Per-warp queue (in shared memory) of the samples the certified path
+// leaves to the exact path.  Kept per warp, so that filling and draining it
+// needs no block barrier; a warp drains it when another round could
+// overflow it and at the end of its piece.
+constexpr int kWarpQueue = 64;
+
+// Appends t for the lanes with `push` to the warp's queue q holding qn
+// entries; returns the new count.  All 32 lanes must call; qn is the same
+// in every lane.
+__device__ __forceinline__ int warp_enqueue(int *q, int qn, bool push, int t) {
+    const unsigned m = __ballot_sync(0xffffffffu, push);
+    if (push) q[qn + __popc(m & ((1u << (threadIdx.x & 31)) - 1u))] = t;
+    return qn + __popc(m);
+}
+
 // Bounds of |double-float value - reference float64 value|.
 constexpr float kEpsPix = 1e-7f;        // pixel coordinate units
 constexpr float kEpsPf = 1e-11f;        // spin factors (values of order 1)

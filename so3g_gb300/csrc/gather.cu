@@ -4,8 +4,9 @@
 //
 // CAR, TAN, ZEA and SIN with flat pixelizors use the certified double-float
 // pointing of fastpoint.cuh (when GatherArgs::fast is set);
-// samples it cannot certify are queued in shared memory and finished by the
-// exact float64 pointing, so every sample's result equals the exact path's.
+// samples it cannot certify are queued in shared memory (per warp) and
+// finished by the exact float64 pointing, so every sample's result equals
+// the exact path's.
 
 #include "host.h"
 
@@ -13,7 +14,6 @@ namespace so3g {
 
 namespace {
 
-constexpr int kQueueCap = 512;
 
 struct GatherArgs {
     DGeom g;
@@ -77,8 +77,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_from_map(GatherArgs a) {
         (P == PX_FLAT_NT_NN || P == PX_FLAT_T_NN || P == PX_FLAT_NT_BL ||
          P == PX_FLAT_T_BL) ||
         (C == SO3G_COORD_CAR && (P == PX_HP_NT || P == PX_HP_T));
-    __shared__ int s_queue[kFastOK ? kQueueCap : 1];
-    __shared__ int s_qn;
+    __shared__ int s_queue[kFastOK ? (kBlock / 32) * kWarpQueue : 1];
     int det, t0, t1;
     if (!seg_piece(a.segs, a.piece, det, t0, t1)) return;
     const QuatD ofs = load_quat(a.dets + 4LL * det);
@@ -91,11 +90,12 @@ __global__ void __launch_bounds__(kBlock, 5) k_from_map(GatherArgs a) {
     }
     dfl qd[4] = {df_from_double(ofs.a), df_from_double(ofs.b), df_from_double(ofs.c),
                  df_from_double(ofs.d)};
-    if (threadIdx.x == 0) s_qn = 0;
-    __syncthreads();
+    int *wq = s_queue + (threadIdx.x >> 5) * kWarpQueue;
+    int qn = 0;
     const int rounds = (t1 - t0 + blockDim.x - 1) / blockDim.x;
     for (int r = 0; r < rounds; r++) {
         const int t = t0 + r * blockDim.x + threadIdx.x;
+        bool push = false;
         if (t < t1) {
             const double *bp = a.bore + 4LL * t;
             const double2 lo = __ldg(reinterpret_cast<const double2 *>(bp));
@@ -128,16 +128,15 @@ __global__ void __launch_bounds__(kBlock, 5) k_from_map(GatherArgs a) {
                 }
                 if (ok) *sp = s;
             }
-            if (!ok) s_queue[atomicAdd(&s_qn, 1)] = t;
+            push = !ok;
         }
-        __syncthreads();
-        const int qn = s_qn;
-        if (qn > kQueueCap - (int)blockDim.x || r == rounds - 1) {
-            for (int i = threadIdx.x; i < qn; i += blockDim.x)
-                exact_gather<C, P>(a, det, s_queue[i], ofs, T, Pr);
-            __syncthreads();
-            if (threadIdx.x == 0) s_qn = 0;
-            __syncthreads();
+        qn = warp_enqueue(wq, qn, push, t);
+        if (qn > kWarpQueue - 32 || r == rounds - 1) {
+            __syncwarp();
+            for (int i = threadIdx.x & 31; i < qn; i += 32)
+                exact_gather<C, P>(a, det, wq[i], ofs, T, Pr);
+            __syncwarp();
+            qn = 0;
         }
     }
 }

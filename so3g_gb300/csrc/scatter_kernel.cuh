@@ -11,9 +11,9 @@
 //
 // Pointing: CAR, TAN, ZEA and SIN with flat pixelizors use the certified
 // double-float pointing of fastpoint.cuh when ScatterArgs::fast is set;
-// samples it cannot certify are queued in shared memory and recomputed by
-// the exact float64 pointing, with plain atomics, when the queue fills and
-// at the end of the piece.  Every other case uses the exact pointing.
+// samples it cannot certify are queued in shared memory (per warp) and
+// recomputed by the exact float64 pointing, with plain atomics, when the
+// queue fills and at the end of the piece.  Every other case uses the exact pointing.
 #pragma once
 
 #include "host.h"
@@ -25,7 +25,6 @@ namespace so3g {
 // its own instantiations.
 namespace {
 
-constexpr int kQueueCap = 512;
 // Resident blocks per SM the scatter kernels are compiled for (caps their
 // registers at 65536 / (kBlock * 5) = 51).
 constexpr int kScatterBlocksPerSM = 5;
@@ -129,10 +128,11 @@ __device__ void exact_sample(const ScatterArgs &a, int det, int t, const QuatD &
 }
 
 // Samples [t0, t1) of detector `det`; every thread of the block calls it
-// with the same arguments.  s_queue/s_qn: the block's shared fallback queue.
+// with the same arguments.  s_queue: the block's fallback queues, kWarpQueue
+// entries per warp.
 template <int C, int P, bool WEIGHT>
 __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int t0, int t1,
-                                              int *s_queue, int &s_qn) {
+                                              int *s_queue) {
     constexpr bool kFastOK = FastEligible<C, P>::value;
     float det_wt = 1.f;
     if (a.det_weights) {
@@ -148,13 +148,13 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
     const unsigned vmask = value_slots<WEIGHT>(nc, mult);
     const bool fast = kFastOK && a.fast;
     dfl qd[4];
+    int *wq = s_queue + (threadIdx.x >> 5) * kWarpQueue;
+    int qn = 0;
     if (kFastOK && fast) {
         qd[0] = df_from_double(ofs.a);
         qd[1] = df_from_double(ofs.b);
         qd[2] = df_from_double(ofs.c);
         qd[3] = df_from_double(ofs.d);
-        if (threadIdx.x == 0) s_qn = 0;
-        __syncthreads();
     }
     const int rounds = (t1 - t0 + blockDim.x - 1) / blockDim.x;
     for (int r = 0; r < rounds; r++) {
@@ -165,6 +165,7 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
         float w[NT];
         int n = 0;
         float sig = 0.f;
+        bool push = false;
         if (live) {
             bool done = false;
             if (kFastOK && fast) {
@@ -176,7 +177,7 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
                           df_split(hi.x, qb[2]) & df_split(hi.y, qb[3]);
                 if (!(ok && fast_pointing<C, P>(a.g, a.ft, a.fc, qb, qd, nc, T, Pr, pix, w, n,
                                                 pf))) {
-                    s_queue[atomicAdd(&s_qn, 1)] = t;
+                    push = true;
                     n = 0;
                 }
                 done = true;
@@ -189,6 +190,7 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
             }
             if (!WEIGHT && n > 0) sig = __ldg(a.signal + det * a.sig_stride + t);
         }
+        if (kFastOK && fast) qn = warp_enqueue(wq, qn, push, t);
 #pragma unroll
         for (int k = 0; k < NT; k++) {
             long long off = -1, plane = 0;
@@ -213,28 +215,22 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
                     if ((vmask >> s) & 1u) atomicAdd(a.map + off + mult[s] * plane, f2d(v[s]));
             }
         }
-        if (kFastOK && fast) {
-            __syncthreads();
-            const int qn = s_qn;
-            if (qn > kQueueCap - (int)blockDim.x || r == rounds - 1) {
-                for (int i = threadIdx.x; i < qn; i += blockDim.x)
-                    exact_sample<C, P, WEIGHT>(a, det, s_queue[i], ofs, T, Pr, det_wt, mult,
-                                               vmask);
-                __syncthreads();
-                if (threadIdx.x == 0) s_qn = 0;
-                __syncthreads();
-            }
+        if (kFastOK && fast && (qn > kWarpQueue - 32 || r == rounds - 1)) {
+            __syncwarp();
+            for (int i = threadIdx.x & 31; i < qn; i += 32)
+                exact_sample<C, P, WEIGHT>(a, det, wq[i], ofs, T, Pr, det_wt, mult, vmask);
+            __syncwarp();
+            qn = 0;
         }
     }
 }
 
 template <int C, int P, bool WEIGHT>
 __global__ void __launch_bounds__(kBlock, kScatterBlocksPerSM) k_scatter(ScatterArgs a) {
-    __shared__ int s_queue[FastEligible<C, P>::value ? kQueueCap : 1];
-    __shared__ int s_qn;
+    __shared__ int s_queue[FastEligible<C, P>::value ? (kBlock / 32) * kWarpQueue : 1];
     int det, t0, t1;
     if (!seg_piece(a.segs, a.piece, det, t0, t1)) return;
-    scatter_piece<C, P, WEIGHT>(a, det, t0, t1, s_queue, s_qn);
+    scatter_piece<C, P, WEIGHT>(a, det, t0, t1, s_queue);
 }
 
 }  // namespace
