@@ -50,6 +50,14 @@ CONFIGS = {
                  az_spread=90., radius=1.5, shape=(4000, 4000), res_arcmin=1.8, noise=False),
 }
 METRIC = "to_map/from_map TOD samples/s (CAR TQU) mixed vs FP64 GPU path, % HBM peak"
+POINTING = {"exact": 0, "certified": 1, "mixed": 2}
+PRECISION = {
+    "mixed": "float32 pointing with certified pixel indices (double-float, then float64, "
+             "fallback), float32 spin factors and products, float64 map accumulation",
+    "certified": "pointing certified equal to float64 (double-float with float64 fallback), "
+                 "float32 products, float64 map accumulation",
+    "exact": "float64 pointing, float32 products, float64 map accumulation",
+}
 ARCMIN = np.pi / 180 / 60
 
 
@@ -70,6 +78,8 @@ def parse():
     ap.add_argument("--batch-scale", type=float, default=1.0,
                     help="cfg4: scale every observation's sample count")
     ap.add_argument("--tiled", action="store_true", help="cfg3: the Tiled NEST variant")
+    ap.add_argument("--pointing", default="mixed", choices=["mixed", "certified", "exact"],
+                    help="pointing mode of the timed steps")
     return ap.parse_args()
 
 
@@ -351,19 +361,45 @@ def run_ours(args, c, rank, world):
         op_ms = {op: float(np.mean([a.elapsed_time(b) for a, b in v])) for op, v in per.items()}
         return total_ms / steps, op_ms, launches, clk.summary()
 
-    ms, op_ms, launches, clocks = timed(_abi.ACCUM_WARP_RUNS, args.steps, args.warmup)
+    mode = POINTING[args.pointing]
+    ms, op_ms, launches, clocks = timed(_abi.ACCUM_WARP_RUNS, args.steps, args.warmup,
+                                        pointing=mode)
     if world > 1:
         t = torch.tensor([ms], device=dev, dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     res = {"ms_per_step": ms, "op_ms": op_ms, "launches": launches, "clocks": clocks}
+    if world == 1 and c["kind"] != "zea_grad" and mode != _abi.POINTING_CERTIFIED:
+        # The bit-exact certified mode, for comparison.
+        msc, opc, _, _ = timed(_abi.ACCUM_WARP_RUNS, max(1, args.steps // 2), 1,
+                               pointing=_abi.POINTING_CERTIFIED)
+        res["certified"] = {"ms_per_step": msc, "op_ms": opc}
     if not args.no_fp64_path and world == 1 and c["kind"] == "car":
         # The plain float64 GPU path: exact float64 pointing, one float64
         # atomic per term.
         ms64, op64, _, _ = timed(_abi.ACCUM_ATOMIC, max(1, args.steps // 2), 1,
                                  pointing=_abi.POINTING_EXACT)
-        eng.pointing = _abi.POINTING_CERTIFIED
         res["fp64_path"] = {"ms_per_step": ms64, "op_ms": op64}
+    if world == 1 and c["kind"] != "zea_grad" and mode != _abi.POINTING_EXACT:
+        # Accuracy of the timed mode against the float64 path on this
+        # workload: to_map maps, and from_map signals of the same map.
+        eng.pointing = _abi.POINTING_EXACT
+        m_ex = eng.to_map(eng.zeros(3, device=dev), q_d, dets_d, resp_d, sig, None, None)
+        s_ex = eng.from_map(m_ex, q_d, dets_d, resp_d, None)
+        eng.pointing = mode
+        m_md = eng.to_map(eng.zeros(3, device=dev), q_d, dets_d, resp_d, sig, None, None)
+        s_md = eng.from_map(m_ex, q_d, dets_d, resp_d, None)
+
+        def rel(a, b):
+            if isinstance(a, list):
+                a = torch.cat([t.reshape(-1) for t in a])
+                b = torch.cat([t.reshape(-1) for t in b])
+            return float((a.double() - b.double()).abs().max() / a.double().abs().max())
+        res["accuracy"] = {"to_map_max_rel_err": rel(m_ex, m_md),
+                           "from_map_max_rel_err": rel(s_ex, s_md),
+                           "reference": "float64 GPU path (exact pointing)"}
+        del m_ex, s_ex, m_md, s_md
+    eng.pointing = mode
     # to_weight_map, timed on its own (not part of the step).
     if world == 1:
         for _ in range(2):
@@ -651,9 +687,10 @@ def main():
     cfg = {"workload": workload, "n_det": c["n_det"], "n_time": c["n_time"],
            "map": map_shape, "step": step_name,
            "l2": "inputs larger than L2 (TOD %.1f GB)" % (c["n_det"] * c["n_time"] * 4 / 1e9),
-           "precision": ("pointing certified equal to float64 (double-float with float64 "
-                         "fallback)" if c["kind"] == "car" else "float64 pointing") +
-                        ", float32 products, float64 map accumulation",
+           "precision": PRECISION[args.pointing] + (
+               "" if c["kind"] == "car" or args.pointing != "mixed" else
+               " (mixed applies to CAR nearest neighbour; this pixelization runs certified)"),
+           "pointing": args.pointing,
            "parallelism": "replicas" if world > 1 else "single GPU"}
 
     if args.impl == "reference":
@@ -696,6 +733,11 @@ def main():
                                      else None),
                          "bytes_per_sample": B, "peak_kind": kind},
             "clocks": res["clocks"], "gpu_launches": int(res["launches"])}
+    if "certified" in res:
+        f = res["certified"]
+        line["certified"] = {"value": N / (f["ms_per_step"] * 1e-3), "op_ms": f["op_ms"]}
+    if "accuracy" in res:
+        line["accuracy"] = res["accuracy"]
     if "fp64_path" in res:
         f = res["fp64_path"]
         line["fp64_path"] = {"value": N / (f["ms_per_step"] * 1e-3), "op_ms": f["op_ms"],

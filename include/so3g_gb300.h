@@ -88,12 +88,21 @@ enum so3g_accum {
 enum so3g_pointing {
     /* Float64 throughout, in the reference's operation order. */
     SO3G_POINTING_EXACT = 0,
-    /* CAR with nearest-neighbour flat pixelizors: double-float pointing
-     * whose pixel indices and float32 spin factors are certified equal to
-     * the exact ones, with the exact path for every sample that cannot be
-     * certified -- the results are those of SO3G_POINTING_EXACT.  Other
-     * pixelizations use the exact path. */
-    SO3G_POINTING_CERTIFIED = 1
+    /* CAR, TAN, ZEA and SIN with flat pixelizors, and HEALPix:
+     * double-float pointing whose pixel indices and float32 spin factors
+     * are certified equal to the exact ones, with the exact path for every
+     * sample that cannot be certified.  Results are those of
+     * SO3G_POINTING_EXACT, except bilinear interpolation weights, which may
+     * differ from it by one float32 ulp.  Other pixelizations use the
+     * exact path. */
+    SO3G_POINTING_CERTIFIED = 1,
+    /* Mixed precision (CAR with nearest-neighbour flat pixelizors; other
+     * pixelizations as SO3G_POINTING_CERTIFIED): float32 pointing whose
+     * pixel indices are certified equal to the exact ones (samples that
+     * cannot be certified take the double-float, then the exact path).
+     * Spin factors and from_map terms are float32 evaluations: maps and
+     * signals agree with the exact path to ~1e-7 of their scale. */
+    SO3G_POINTING_MIXED = 2
 };
 
 /* Status codes returned by every entry point. */

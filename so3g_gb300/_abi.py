@@ -19,7 +19,7 @@ INTERP_NEAREST, INTERP_BILINEAR = 0, 1
 ACCUM_ATOMIC, ACCUM_WARP_RUNS = 0, 1
 DEVERR_NONE, DEVERR_MISSING_TILE, DEVERR_PIXEL_RANGE = 0, 1, 2
 ABI_VERSION = 2
-POINTING_EXACT, POINTING_CERTIFIED = 0, 1
+POINTING_EXACT, POINTING_CERTIFIED, POINTING_MIXED = 0, 1, 2
 LUT_N = 1 << 14
 
 c_int32 = ctypes.c_int32

@@ -120,6 +120,22 @@ FastConst make_fast_const(const DGeom &g) {
     return c;
 }
 
+MixedConst make_mixed_const(const DGeom &g) {
+    MixedConst c;
+    c.inv_cdx = g.cdx != 0. ? (float)(1. / g.cdx) : 0.f;
+    c.inv_cdy = g.cdy != 0. ? (float)(1. / g.cdy) : 0.f;
+    c.off_x = (float)(g.crx - 1 + 0.5);
+    c.off_y = (float)(g.cry - 1 + 0.5);
+    c.pi = (float)kPi;
+    c.half_pi = (float)(kPi / 2);
+    return c;
+}
+
+int fast_mode(const so3g_pixelization *pz, const FastTables &ft) {
+    if (!ft.asin_t) return SO3G_POINTING_EXACT;
+    return pz->pointing;
+}
+
 int pix_kind(const so3g_pixelization *pz) {
     if (pz->pix_sys == SO3G_PIX_HEALPIX) return pz->tiled ? PX_HP_T : PX_HP_NT;
     return (pz->tiled ? 2 : 0) + (pz->interp == SO3G_INTERP_BILINEAR ? 1 : 0);
@@ -146,6 +162,9 @@ int make_geom_lut(const so3g_pixelization *pz, DGeom *g, const double *lut) {
         return set_error(SO3G_ERR_ARGUMENT, "unknown coordinate system %d", pz->coord_sys);
     if (pz->interp != SO3G_INTERP_NEAREST && pz->interp != SO3G_INTERP_BILINEAR)
         return set_error(SO3G_ERR_ARGUMENT, "unknown interpolation %d", pz->interp);
+    if (pz->pointing != SO3G_POINTING_EXACT && pz->pointing != SO3G_POINTING_CERTIFIED &&
+        pz->pointing != SO3G_POINTING_MIXED)
+        return set_error(SO3G_ERR_ARGUMENT, "unknown pointing mode %d", pz->pointing);
     g->ncomp = pz->n_comp;
     g->lut = lut;
     if (pz->pix_sys == SO3G_PIX_HEALPIX) {

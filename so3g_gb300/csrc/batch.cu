@@ -13,11 +13,11 @@ namespace so3g {
 
 namespace {
 
-template <int C, int P, bool WEIGHT>
+template <int C, int P, bool WEIGHT, int MODE>
 __global__ void __launch_bounds__(kBlock, kScatterBlocksPerSM)
     k_scatter_batch(ScatterArgs base, const so3g_obs *obs, int n_obs,
                     const long long *work_off, long long n_work) {
-    __shared__ int s_queue[FastEligible<C, P>::value ? (kBlock / 32) * kWarpQueue : 1];
+    __shared__ int s_queue[QueueInts<C, P, MODE>::value];
     for (long long w = blockIdx.x; w < n_work; w += gridDim.x) {
         // The observation holding item w: largest o with work_off[o] <= w.
         int lo = 0, hi = n_obs - 1;
@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(kBlock, kScatterBlocksPerSM)
         a.signal = ob.signal;
         a.sig_stride = ob.sig_det_stride;
         a.det_weights = ob.det_weights;
-        scatter_piece<C, P, WEIGHT>(a, det, t0, t1, s_queue);
+        scatter_piece<C, P, WEIGHT, MODE>(a, det, t0, t1, s_queue);
     }
 }
 
@@ -60,24 +60,34 @@ struct BatchLaunch {
     cudaStream_t stream;
     int sms;
     template <int C, int P>
-    int run() {
-        long long grid = blocks;
-        if (blocks < 0) {
-            // One block per work item, scheduled by the hardware.
-            grid = n_work;
-        } else if (blocks == 0) {
-            // One full wave: every block resident at once.
-            int per_sm = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scatter_batch<C, P, WEIGHT>,
-                                                          kBlock, 0);
-            grid = (per_sm > 0 ? per_sm : 1) * sms;
+    struct Go {
+        BatchLaunch *L;
+        template <int MODE>
+        int go() {
+            long long grid = L->blocks;
+            if (L->blocks < 0) {
+                // One block per work item, scheduled by the hardware.
+                grid = L->n_work;
+            } else if (L->blocks == 0) {
+                // One full wave: every block resident at once.
+                int per_sm = 0;
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                    &per_sm, k_scatter_batch<C, P, WEIGHT, MODE>, kBlock, 0);
+                grid = (long long)(per_sm > 0 ? per_sm : 1) * L->sms;
+            }
+            if (grid > L->n_work) grid = L->n_work;
+            if (grid > 0x7fffffffLL)
+                return set_error(SO3G_ERR_RANGE, "batch of %lld work items: too many blocks",
+                                 grid);
+            k_scatter_batch<C, P, WEIGHT, MODE><<<(unsigned)grid, kBlock, 0, L->stream>>>(
+                L->a, L->obs, L->n_obs, L->work_off, L->n_work);
+            return after_launch(WEIGHT ? "to_weight_map batch" : "to_map batch");
         }
-        if (grid > n_work) grid = n_work;
-        if (grid > 0x7fffffffLL)
-            return set_error(SO3G_ERR_RANGE, "batch of %lld work items: too many blocks", grid);
-        k_scatter_batch<C, P, WEIGHT><<<(unsigned)grid, kBlock, 0, stream>>>(a, obs, n_obs,
-                                                                               work_off, n_work);
-        return after_launch(WEIGHT ? "to_weight_map batch" : "to_map batch");
+    };
+    template <int C, int P>
+    int run() {
+        Go<C, P> g{this};
+        return by_mode<C, P>(a.fast, g);
     }
 };
 
@@ -116,7 +126,8 @@ int batch_entry(const so3g_pixelization *pz, const so3g_obs *obs, int32_t n_obs,
     L.a.map = map->data;
     L.a.ft = device_fast_tables();
     L.a.fc = make_fast_const(L.a.g);
-    L.a.fast = (pz->pointing == SO3G_POINTING_CERTIFIED && L.a.ft.asin_t) ? 1 : 0;
+    L.a.mc = make_mixed_const(L.a.g);
+    L.a.fast = fast_mode(pz, L.a.ft);
     L.obs = obs;
     L.n_obs = n_obs;
     L.work_off = reinterpret_cast<const long long *>(work_offset);

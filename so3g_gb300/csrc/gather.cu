@@ -26,9 +26,10 @@ struct GatherArgs {
     Segs segs;
     int piece;
     int *err;
-    int fast;
+    int fast;           // SO3G_POINTING_*: 0 exact, 1 certified, 2 mixed
     FastTables ft;
     FastConst fc;
+    MixedConst mc;
 };
 
 // Adds the sample's map terms to its signal (src/Projection.cxx:1763-1765).
@@ -68,34 +69,134 @@ __device__ void exact_gather(const GatherArgs &a, int det, int t, const QuatD &o
     gather_taps<P, NT>(a, a.signal + det * a.sig_stride + t, n, pix, w, pf);
 }
 
+// One sample through the certified double-float pointing and certified
+// float32 roundings of each term; false (signal untouched) when anything is
+// not certain.
 template <int C, int P>
-// Compiled for 5 resident blocks per SM (at most 51 registers).
+__device__ bool df_gather(const GatherArgs &a, int det, int t, const dfl (&qd)[4], float T,
+                          float Pr) {
+    constexpr int NT = PixTraits<P>::taps;
+    const double *bp = a.bore + 4LL * t;
+    const double2 lo = __ldg(reinterpret_cast<const double2 *>(bp));
+    const double2 hi = __ldg(reinterpret_cast<const double2 *>(bp) + 1);
+    dfl qb[4];
+    if (!(df_split(lo.x, qb[0]) & df_split(lo.y, qb[1]) & df_split(hi.x, qb[2]) &
+          df_split(hi.y, qb[3])))
+        return false;
+    int pix[NT][3];
+    float pf[3], w[NT];
+    int n = 0;
+    const int nc = a.g.ncomp;
+    if (!fast_pointing<C, P>(a.g, a.ft, a.fc, qb, qd, nc, T, Pr, pix, w, n, pf)) return false;
+    if (n == 0) return true;
+    float *sp = a.signal + det * a.sig_stride + t;
+    float s = *sp;
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < NT; k++) {
+        if (k >= n || !ok) break;
+        long long off, plane;
+        const int bad = locate<P>(a.g, pix[k], &off, &plane);
+        if (bad >= 0) {
+            record_missing_tile(a.err, bad);
+            continue;
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+            if (ok && c < nc) ok = fast_accum(s, __ldg(a.map + off + c * plane), pf[c], w[k]);
+    }
+    if (ok) *sp = s;
+    return ok;
+}
+
+// Compiled for 5 resident blocks per SM (at most 51 registers), one
+// variant per pointing mode (0 exact, 1 certified, 2 mixed).
+template <int C, int P, int MODE>
 __global__ void __launch_bounds__(kBlock, 5) k_from_map(GatherArgs a) {
-    constexpr bool kFastOK =
-        (C == SO3G_COORD_CAR || C == SO3G_COORD_TAN || C == SO3G_COORD_ZEA ||
-         C == SO3G_COORD_SIN) &&
-        (P == PX_FLAT_NT_NN || P == PX_FLAT_T_NN || P == PX_FLAT_NT_BL ||
-         P == PX_FLAT_T_BL) ||
-        (C == SO3G_COORD_CAR && (P == PX_HP_NT || P == PX_HP_T));
-    __shared__ int s_queue[kFastOK ? (kBlock / 32) * kWarpQueue : 1];
+    constexpr bool kFastOK = FastEligible<C, P>::value && MODE >= 1;
+    constexpr bool kMixedOK = MixedEligible<C, P>::value && MODE == 2;
+    __shared__ int s_queue[!kFastOK ? 1 : (kMixedOK ? 2 : 1) * (kBlock / 32) * kWarpQueue];
     int det, t0, t1;
     if (!seg_piece(a.segs, a.piece, det, t0, t1)) return;
     const QuatD ofs = load_quat(a.dets + 4LL * det);
     const float T = __ldg(a.resp + 2 * det), Pr = __ldg(a.resp + 2 * det + 1);
     const int nc = a.g.ncomp;
     constexpr int NT = PixTraits<P>::taps;
-    if (!(kFastOK && a.fast)) {
+    if (!kFastOK) {
         for (int t = t0 + threadIdx.x; t < t1; t += blockDim.x) exact_gather<C, P>(a, det, t, ofs, T, Pr);
         return;
     }
     dfl qd[4] = {df_from_double(ofs.a), df_from_double(ofs.b), df_from_double(ofs.c),
                  df_from_double(ofs.d)};
+    constexpr bool mixed = kMixedOK;
+    float qd32[4];
+    if (kMixedOK && mixed) {
+        qd32[0] = __double2float_rn(ofs.a);
+        qd32[1] = __double2float_rn(ofs.b);
+        qd32[2] = __double2float_rn(ofs.c);
+        qd32[3] = __double2float_rn(ofs.d);
+    }
     int *wq = s_queue + (threadIdx.x >> 5) * kWarpQueue;
-    int qn = 0;
+    int *wdf = s_queue + ((kBlock >> 5) + (threadIdx.x >> 5)) * kWarpQueue;
+    int qn = 0, qdf = 0;
+    auto drain_exact = [&]() {
+        __syncwarp();
+        for (int i = threadIdx.x & 31; i < qn; i += 32)
+            exact_gather<C, P>(a, det, wq[i], ofs, T, Pr);
+        __syncwarp();
+        qn = 0;
+    };
     const int rounds = (t1 - t0 + blockDim.x - 1) / blockDim.x;
     for (int r = 0; r < rounds; r++) {
         const int t = t0 + r * blockDim.x + threadIdx.x;
-        bool push = false;
+        bool push = false, push_df = false;
+        if (kMixedOK && mixed) {
+            if (t < t1) {
+                const double *bp = a.bore + 4LL * t;
+                const double2 lo = __ldg(reinterpret_cast<const double2 *>(bp));
+                const double2 hi = __ldg(reinterpret_cast<const double2 *>(bp) + 1);
+                const float qb[4] = {d2f_trunc(lo.x), d2f_trunc(lo.y), d2f_trunc(hi.x),
+                                     d2f_trunc(hi.y)};
+                int pix[3];
+                float pf[3];
+                bool on = false;
+                if (mixed_car<P>(a.g, a.ft, a.mc, qb, qd32, nc, T, Pr, pix, on, pf)) {
+                    if (on) {
+                        long long off, plane;
+                        const int bad = locate<P>(a.g, pix, &off, &plane);
+                        if (bad >= 0) {
+                            record_missing_tile(a.err, bad);
+                        } else {
+                            // float32 terms (the mixed-precision contract).
+                            float *sp = a.signal + det * a.sig_stride + t;
+                            float s = *sp;
+#pragma unroll
+                            for (int c = 0; c < 3; c++)
+                                if (c < nc)
+                                    s = fmaf(d2f_trunc(__ldg(a.map + off + c * plane)), pf[c], s);
+                            *sp = s;
+                        }
+                    }
+                } else {
+                    push_df = true;
+                }
+            }
+            qdf = warp_enqueue(wdf, qdf, push_df, t);
+            if (qdf >= 32 || (r == rounds - 1 && qdf > 0)) {
+                __syncwarp();
+                for (int base = 0; base < qdf; base += 32) {
+                    const int i = base + (threadIdx.x & 31);
+                    const int ts = i < qdf ? wdf[i] : 0;
+                    const bool px = i < qdf && !df_gather<C, P>(a, det, ts, qd, T, Pr);
+                    qn = warp_enqueue(wq, qn, px, ts);
+                    if (qn > kWarpQueue - 32) drain_exact();
+                }
+                __syncwarp();
+                qdf = 0;
+            }
+            if (qn > kWarpQueue - 32 || r == rounds - 1) drain_exact();
+            continue;
+        }
         if (t < t1) {
             const double *bp = a.bore + 4LL * t;
             const double2 lo = __ldg(reinterpret_cast<const double2 *>(bp));
@@ -131,13 +232,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_from_map(GatherArgs a) {
             push = !ok;
         }
         qn = warp_enqueue(wq, qn, push, t);
-        if (qn > kWarpQueue - 32 || r == rounds - 1) {
-            __syncwarp();
-            for (int i = threadIdx.x & 31; i < qn; i += 32)
-                exact_gather<C, P>(a, det, wq[i], ofs, T, Pr);
-            __syncwarp();
-            qn = 0;
-        }
+        if (qn > kWarpQueue - 32 || r == rounds - 1) drain_exact();
     }
 }
 
@@ -146,9 +241,18 @@ struct GatherLaunch {
     dim3 grid;
     cudaStream_t stream;
     template <int C, int P>
+    struct Go {
+        GatherLaunch *L;
+        template <int MODE>
+        int go() {
+            k_from_map<C, P, MODE><<<L->grid, kBlock, 0, L->stream>>>(L->a);
+            return after_launch("from_map");
+        }
+    };
+    template <int C, int P>
     int run() {
-        k_from_map<C, P><<<grid, kBlock, 0, stream>>>(a);
-        return after_launch("from_map");
+        Go<C, P> g{this};
+        return by_mode<C, P>(a.fast, g);
     }
 };
 
@@ -182,7 +286,8 @@ extern "C" int so3g_proj_from_map(const so3g_pixelization *pz, const double *bor
     L.a.err = err;
     L.a.ft = device_fast_tables();
     L.a.fc = make_fast_const(L.a.g);
-    L.a.fast = (pz->pointing == SO3G_POINTING_CERTIFIED && L.a.ft.asin_t) ? 1 : 0;
+    L.a.mc = make_mixed_const(L.a.g);
+    L.a.fast = fast_mode(pz, L.a.ft);
     L.grid = dim3((unsigned)n_det, (unsigned)((n_time + L.a.piece - 1) / L.a.piece));
     L.stream = (cudaStream_t)stream;
     return dispatch_cp(pz->coord_sys, pix_kind(pz), L);

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include "../../include/so3g_gb300.h"
 #include "fastpoint.cuh"
+#include "mixedpoint.cuh"
 
 namespace so3g {
 
@@ -29,6 +30,11 @@ const double *host_lut();
 FastTables device_fast_tables();
 // Double-float pixelizor constants of the certified pointing.
 FastConst make_fast_const(const DGeom &g);
+// Float32 pixelizor constants of the mixed pointing.
+MixedConst make_mixed_const(const DGeom &g);
+// The pointing mode a kernel runs for a pixelization (0 exact, 1 certified,
+// 2 mixed): the exact path when the double-float tables are missing.
+int fast_mode(const so3g_pixelization *pz, const FastTables &ft);
 // Adds the map's tile table to the geometry; checks the tile count.
 int attach_map(const so3g_pixelization *pz, const so3g_map *m, DGeom *g);
 // Pixelizor kind (PX_*) of a pixelization.

@@ -82,7 +82,7 @@ struct NoAllocLaunch {
     cudaStream_t stream;
     template <int C, int P>
     int run() {
-        k_scatter<C, P, false><<<grid, kBlock, 0, stream>>>(a);
+        k_scatter<C, P, false, SO3G_POINTING_EXACT><<<grid, kBlock, 0, stream>>>(a);
         return after_launch("to_map (no-alloc)");
     }
 };

@@ -14,9 +14,18 @@ struct ScatterLaunch {
     dim3 grid;
     cudaStream_t stream;
     template <int C, int P>
+    struct Go {
+        ScatterLaunch *L;
+        template <int MODE>
+        int go() {
+            k_scatter<C, P, WEIGHT, MODE><<<L->grid, kBlock, 0, L->stream>>>(L->a);
+            return after_launch(WEIGHT ? "to_weight_map" : "to_map");
+        }
+    };
+    template <int C, int P>
     int run() {
-        k_scatter<C, P, WEIGHT><<<grid, kBlock, 0, stream>>>(a);
-        return after_launch(WEIGHT ? "to_weight_map" : "to_map");
+        Go<C, P> g{this};
+        return by_mode<C, P>(a.fast, g);
     }
 };
 
@@ -54,7 +63,8 @@ int scatter_entry(const so3g_pixelization *pz, const double *bore, int32_t n_tim
     L.a.map = map->data;
     L.a.ft = device_fast_tables();
     L.a.fc = make_fast_const(L.a.g);
-    L.a.fast = (pz->pointing == SO3G_POINTING_CERTIFIED && L.a.ft.asin_t) ? 1 : 0;
+    L.a.mc = make_mixed_const(L.a.g);
+    L.a.fast = fast_mode(pz, L.a.ft);
     L.grid = dim3((unsigned)n_seg, (unsigned)((max_len + L.a.piece - 1) / L.a.piece));
     L.stream = (cudaStream_t)stream;
     return dispatch_cp(pz->coord_sys, pix_kind(pz), L);

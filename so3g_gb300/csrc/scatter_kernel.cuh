@@ -18,6 +18,7 @@
 
 #include "host.h"
 #include "fastpoint.cuh"
+#include "mixedpoint.cuh"
 
 namespace so3g {
 
@@ -42,20 +43,12 @@ struct ScatterArgs {
     int accum;
     int *err;
     double *map;
-    int fast;
+    int fast;           // SO3G_POINTING_*: 0 exact, 1 certified, 2 mixed
     FastTables ft;
     FastConst fc;
+    MixedConst mc;
 };
 
-template <int C, int P>
-struct FastEligible {
-    static constexpr bool value =
-        (C == SO3G_COORD_CAR || C == SO3G_COORD_TAN || C == SO3G_COORD_ZEA ||
-         C == SO3G_COORD_SIN) &&
-        (P == PX_FLAT_NT_NN || P == PX_FLAT_T_NN || P == PX_FLAT_NT_BL ||
-         P == PX_FLAT_T_BL) ||
-        (C == SO3G_COORD_CAR && (P == PX_HP_NT || P == PX_HP_T));
-};
 
 // Value slots: to_map slot c = component c; to_weight_map slots are the
 // upper-triangle pairs (i, j), j >= i, in row order.
@@ -127,13 +120,66 @@ __device__ void exact_sample(const ScatterArgs &a, int det, int t, const QuatD &
     }
 }
 
-// Samples [t0, t1) of detector `det`; every thread of the block calls it
-// with the same arguments.  s_queue: the block's fallback queues, kWarpQueue
-// entries per warp.
+// One sample through the certified double-float pointing, added with plain
+// atomics; false (nothing added) when it is not certified.
 template <int C, int P, bool WEIGHT>
+__device__ bool df_sample(const ScatterArgs &a, int det, int t, const dfl (&qd)[4], float T,
+                          float Pr, float det_wt, const int *mult, unsigned vmask) {
+    constexpr int NT = PixTraits<P>::taps;
+    constexpr int NV = WEIGHT ? 6 : 3;
+    const double *bp = a.bore + 4LL * t;
+    const double2 lo = __ldg(reinterpret_cast<const double2 *>(bp));
+    const double2 hi = __ldg(reinterpret_cast<const double2 *>(bp) + 1);
+    dfl qb[4];
+    if (!(df_split(lo.x, qb[0]) & df_split(lo.y, qb[1]) & df_split(hi.x, qb[2]) &
+          df_split(hi.y, qb[3])))
+        return false;
+    int pix[NT][3];
+    float w[NT], pf[3];
+    int n = 0;
+    if (!fast_pointing<C, P>(a.g, a.ft, a.fc, qb, qd, a.g.ncomp, T, Pr, pix, w, n, pf))
+        return false;
+    const float sig = (!WEIGHT && n > 0) ? __ldg(a.signal + det * a.sig_stride + t) : 0.f;
+    for (int k = 0; k < n; k++) {
+        long long off, plane;
+        int bad = locate<P>(a.g, pix[k], &off, &plane);
+        if (bad >= 0) {
+            record_missing_tile(a.err, bad);
+            continue;
+        }
+        float v[NV];
+        tap_values<WEIGHT>(sig, pf, w[k], det_wt, v);
+#pragma unroll
+        for (int s = 0; s < NV; s++)
+            if ((vmask >> s) & 1u) atomicAdd(a.map + off + mult[s] * plane, f2d(v[s]));
+    }
+    return true;
+}
+
+// Pointing variant a kernel is compiled for: 0 exact, 1 certified, 2 mixed
+// (the modes a pixelization does not support fall back to the next lower).
+template <int C, int P, int MODE>
+struct PointingVariant {
+    static constexpr bool fast = FastEligible<C, P>::value && MODE >= 1;
+    static constexpr bool mixed = MixedEligible<C, P>::value && MODE == 2;
+};
+
+// Shared ints of a block's fallback queues: per warp, one queue for the
+// exact path and (mixed pointing) one for the double-float path.
+template <int C, int P, int MODE>
+struct QueueInts {
+    static constexpr int value = !PointingVariant<C, P, MODE>::fast ? 1
+                                 : (PointingVariant<C, P, MODE>::mixed ? 2 : 1) *
+                                       (kBlock / 32) * kWarpQueue;
+};
+
+// Samples [t0, t1) of detector `det`; every thread of the block calls it
+// with the same arguments.  s_queue: the block's fallback queues
+// (QueueInts<C, P, MODE> ints).
+template <int C, int P, bool WEIGHT, int MODE>
 __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int t0, int t1,
                                               int *s_queue) {
-    constexpr bool kFastOK = FastEligible<C, P>::value;
+    constexpr bool kFastOK = PointingVariant<C, P, MODE>::fast;
     float det_wt = 1.f;
     if (a.det_weights) {
         det_wt = __ldg(a.det_weights + det);
@@ -146,16 +192,34 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
     constexpr int NV = WEIGHT ? 6 : 3;
     int mult[NV];
     const unsigned vmask = value_slots<WEIGHT>(nc, mult);
-    const bool fast = kFastOK && a.fast;
+    constexpr bool kMixedOK = PointingVariant<C, P, MODE>::mixed;
+    constexpr bool fast = kFastOK;
+    constexpr bool mixed = kMixedOK;
     dfl qd[4];
+    float qd32[4];
     int *wq = s_queue + (threadIdx.x >> 5) * kWarpQueue;
-    int qn = 0;
+    int *wdf = s_queue + ((kBlock >> 5) + (threadIdx.x >> 5)) * kWarpQueue;
+    int qn = 0, qdf = 0;
     if (kFastOK && fast) {
         qd[0] = df_from_double(ofs.a);
         qd[1] = df_from_double(ofs.b);
         qd[2] = df_from_double(ofs.c);
         qd[3] = df_from_double(ofs.d);
     }
+    if (kMixedOK && mixed) {
+        qd32[0] = __double2float_rn(ofs.a);
+        qd32[1] = __double2float_rn(ofs.b);
+        qd32[2] = __double2float_rn(ofs.c);
+        qd32[3] = __double2float_rn(ofs.d);
+    }
+    // Recomputes the exact-path queue with the float64 pointing.
+    auto drain_exact = [&]() {
+        __syncwarp();
+        for (int i = threadIdx.x & 31; i < qn; i += 32)
+            exact_sample<C, P, WEIGHT>(a, det, wq[i], ofs, T, Pr, det_wt, mult, vmask);
+        __syncwarp();
+        qn = 0;
+    };
     const int rounds = (t1 - t0 + blockDim.x - 1) / blockDim.x;
     for (int r = 0; r < rounds; r++) {
         const int t = t0 + r * blockDim.x + threadIdx.x;
@@ -165,10 +229,25 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
         float w[NT];
         int n = 0;
         float sig = 0.f;
-        bool push = false;
+        bool push = false, push_df = false;
         if (live) {
             bool done = false;
-            if (kFastOK && fast) {
+            if (kMixedOK && mixed) {
+                const double *bp = a.bore + 4LL * t;
+                const double2 lo = __ldg(reinterpret_cast<const double2 *>(bp));
+                const double2 hi = __ldg(reinterpret_cast<const double2 *>(bp) + 1);
+                const float qb[4] = {d2f_trunc(lo.x), d2f_trunc(lo.y), d2f_trunc(hi.x),
+                                     d2f_trunc(hi.y)};
+                bool on = false;
+                if (mixed_car<P>(a.g, a.ft, a.mc, qb, qd32, nc, T, Pr, pix[0], on, pf)) {
+                    n = on ? 1 : 0;
+                    w[0] = 1.f;
+                } else {
+                    push_df = true;
+                    n = 0;
+                }
+                done = true;
+            } else if (kFastOK && fast) {
                 const double *bp = a.bore + 4LL * t;
                 const double2 lo = __ldg(reinterpret_cast<const double2 *>(bp));
                 const double2 hi = __ldg(reinterpret_cast<const double2 *>(bp) + 1);
@@ -191,6 +270,7 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
             if (!WEIGHT && n > 0) sig = __ldg(a.signal + det * a.sig_stride + t);
         }
         if (kFastOK && fast) qn = warp_enqueue(wq, qn, push, t);
+        if (kMixedOK && mixed) qdf = warp_enqueue(wdf, qdf, push_df, t);
 #pragma unroll
         for (int k = 0; k < NT; k++) {
             long long off = -1, plane = 0;
@@ -215,23 +295,36 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
                     if ((vmask >> s) & 1u) atomicAdd(a.map + off + mult[s] * plane, f2d(v[s]));
             }
         }
-        if (kFastOK && fast && (qn > kWarpQueue - 32 || r == rounds - 1)) {
+        // Mixed pointing: the samples the float32 tier left, 32 at a time
+        // through the double-float path; what that cannot certify goes on
+        // to the exact queue.
+        if (kMixedOK && mixed && (qdf >= 32 || (r == rounds - 1 && qdf > 0))) {
             __syncwarp();
-            for (int i = threadIdx.x & 31; i < qn; i += 32)
-                exact_sample<C, P, WEIGHT>(a, det, wq[i], ofs, T, Pr, det_wt, mult, vmask);
+            for (int base = 0; base < qdf; base += 32) {
+                const int i = base + (threadIdx.x & 31);
+                const int ts = i < qdf ? wdf[i] : 0;
+                const bool px =
+                    i < qdf && !df_sample<C, P, WEIGHT>(a, det, ts, qd, T, Pr, det_wt, mult,
+                                                        vmask);
+                qn = warp_enqueue(wq, qn, px, ts);
+                if (qn > kWarpQueue - 32) drain_exact();
+            }
             __syncwarp();
-            qn = 0;
+            qdf = 0;
         }
+        if (kFastOK && fast && (qn > kWarpQueue - 32 || r == rounds - 1)) drain_exact();
     }
 }
 
-template <int C, int P, bool WEIGHT>
+template <int C, int P, bool WEIGHT, int MODE>
 __global__ void __launch_bounds__(kBlock, kScatterBlocksPerSM) k_scatter(ScatterArgs a) {
-    __shared__ int s_queue[FastEligible<C, P>::value ? (kBlock / 32) * kWarpQueue : 1];
+    __shared__ int s_queue[QueueInts<C, P, MODE>::value];
     int det, t0, t1;
     if (!seg_piece(a.segs, a.piece, det, t0, t1)) return;
-    scatter_piece<C, P, WEIGHT>(a, det, t0, t1, s_queue);
+    scatter_piece<C, P, WEIGHT, MODE>(a, det, t0, t1, s_queue);
 }
+
+
 
 }  // namespace
 

@@ -29,8 +29,10 @@ INT32_MAX = 2**31 - 1
 # Default scatter accumulator: warp pre-reduction of pixel runs.
 DEFAULT_ACCUM = _abi.ACCUM_WARP_RUNS
 # Default pointing evaluation: certified double-float where available (its
-# results equal the exact float64 path's); set an engine's ``pointing``
-# attribute to _abi.POINTING_EXACT to force float64 everywhere.
+# results equal the exact float64 path's).  An engine's ``pointing``
+# attribute selects another: _abi.POINTING_EXACT (float64 everywhere) or
+# _abi.POINTING_MIXED (float32 pointing with certified pixel indices; maps
+# within ~1e-7 of the float64 path's).
 DEFAULT_POINTING = _abi.POINTING_CERTIFIED
 
 

@@ -1,0 +1,110 @@
+"""Mixed-precision pointing (POINTING_MIXED, CAR nearest neighbour): pixel
+indices bit-identical to the exact float64 path, sample by sample and on
+pixel edges; spin factors, maps and signals within the mixed-precision
+tolerance (1e-6 of their scale) of the exact path."""
+import numpy as np
+import pytest
+
+from so3g_gb300 import _abi, synth
+from conftest import bits_equal
+from test_gpu_certified import _engine, _probe_maps, _quats_at
+
+pytestmark = pytest.mark.gpu
+ARCMIN = np.pi / 180 / 60
+MODES = (_abi.POINTING_EXACT, _abi.POINTING_MIXED)
+
+
+def _probe(eng, q, dets, resp, tiled, ncomp=3):
+    import torch
+    qd, dd, rd = (torch.from_numpy(x).cuda() for x in (q, dets, resp))
+    maps = _probe_maps(eng, tiled, ncomp)
+    out = {}
+    for mode in MODES:
+        eng.pointing = mode
+        out[mode] = [eng.from_map(m, qd, dd, rd, None).cpu().numpy() for m in maps]
+    ex, mx = out[_abi.POINTING_EXACT], out[_abi.POINTING_MIXED]
+    # Pixel index (T probe: 1 + index, exact in float32): bit for bit.
+    assert bits_equal(ex[0], mx[0])
+    # Spin factors: float32 evaluations.
+    for a, b in zip(ex[1:], mx[1:]):
+        assert np.abs(a - b).max() <= 2e-5
+        assert np.abs(a - b).mean() <= 2e-7
+    return ex
+
+
+@pytest.mark.parametrize("tiled", [False, True])
+def test_mixed_pixels_at_scale(tiled):
+    Q, dets, resp, gamma, _ = synth.workload(200, 100_000, seed=51, radius_deg=1.5)
+    p, eng = _engine((700, 900), ARCMIN, tiled)
+    q = synth.native(p, Q)
+    res = _probe(eng, q, dets, resp, tiled)
+    on = res[0] > 0
+    assert 0.5 < on.mean() < 1.0
+
+
+def test_mixed_pixel_edges():
+    rng = np.random.default_rng(53)
+    p, eng = _engine((300, 400), 0.5 * ARCMIN, False)
+    ny, nx, dy, dx, cry, crx = eng.naxis + eng.cdelt + eng.crpix
+    n = 40000
+    ix = rng.integers(-2, nx + 2, n).astype(float)
+    iy = rng.integers(-2, ny + 2, n).astype(float)
+    jit = rng.choice([0., 1e-13, -1e-13, 1e-9, 1e-6, -1e-5, 0.5], n)
+    lon = (ix + jit - crx + 1 - 0.5) * dx
+    lat = (iy + jit - cry + 1 - 0.5) * dy
+    q = _quats_at(lon, lat, rng.uniform(0, np.pi, n))
+    dets = np.array([[1., 0., 0., 0.], [np.cos(0.3), 0., 0., np.sin(0.3)]])
+    resp = np.array([[1., 1.], [0.7, 0.45]], np.float32)
+    _probe(eng, q, dets, resp, False)
+
+
+def test_mixed_wide_map_seam_and_caps():
+    """A map spanning 360 x 180 degrees: the atan2 seam, the octants and
+    the regions beyond the float32 tier's |sin lat| < 0.9 guard."""
+    n = 40000
+    rng = np.random.default_rng(55)
+    lon = np.concatenate([rng.choice([np.pi, -np.pi, np.pi / 4, -3 * np.pi / 4], n // 2) +
+                          rng.choice([0., 1e-12, -1e-12, 1e-7], n // 2),
+                          rng.uniform(-np.pi, np.pi, n // 2)])
+    lat = rng.uniform(-1.5, 1.5, n)
+    q = _quats_at(lon, lat, rng.uniform(0, np.pi, n))
+    dets = np.array([[1., 0., 0., 0.]])
+    resp = np.ones((1, 2), np.float32)
+    p, eng = _engine((200, 200), 60 * ARCMIN, False)
+    eng2 = type(eng)((200, 400, 0.9 * np.pi / 180, -0.9 * np.pi / 180, 100.5, 200.5))
+    _probe(eng2, q, dets, resp, False)
+
+
+@pytest.mark.parametrize("tiled", [False, True])
+def test_mixed_maps_within_tolerance(tiled):
+    import torch
+    Q, dets, resp, gamma, sig = synth.workload(64, 100_000, seed=57, radius_deg=1.0)
+    p, eng = _engine((600, 600), ARCMIN, tiled)
+    q = synth.native(p, Q)
+    qd, dd, rd, sd = (torch.from_numpy(x).cuda() for x in (q, dets, resp, sig))
+
+    def zeros(lead):
+        if not tiled:
+            return torch.zeros(lead + eng._pix_shape(), dtype=torch.float64, device="cuda")
+        return [torch.zeros(lead + eng._tile_pix_shape(i), dtype=torch.float64, device="cuda")
+                for i in range(eng._n_tile())]
+
+    def flat(x):
+        if isinstance(x, list):
+            x = torch.cat([t.reshape(-1) for t in x])
+        return x.reshape(-1).double().cpu().numpy()
+
+    out = {}
+    m_exact = None
+    for mode in MODES:
+        eng.pointing = mode
+        m = eng.to_map(zeros((3,)), qd, dd, rd, sd, None, None)
+        w = eng.to_weight_map(zeros((3, 3)), qd, dd, rd, None, None)
+        if m_exact is None:
+            m_exact = m
+        # from_map of the same (exact) map in both modes.
+        s0 = torch.from_numpy(np.full(sig.shape, 0.25, np.float32)).cuda()
+        back = eng.from_map(m_exact, qd, dd, rd, s0)
+        out[mode] = [flat(x) for x in (m, w, back)]
+    for a, b in zip(out[_abi.POINTING_EXACT], out[_abi.POINTING_MIXED]):
+        assert np.abs(a - b).max() <= 1e-6 * np.abs(a).max()
