@@ -136,6 +136,42 @@ int fast_mode(const so3g_pixelization *pz, const FastTables &ft) {
     return pz->pointing;
 }
 
+namespace {
+__global__ void k_bore_f32(const double *bore, float4 *out, int n_time) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_time) return;
+    const double2 lo = __ldg(reinterpret_cast<const double2 *>(bore + 4LL * t));
+    const double2 hi = __ldg(reinterpret_cast<const double2 *>(bore + 4LL * t) + 1);
+    out[t] = make_float4(__double2float_rn(lo.x), __double2float_rn(lo.y),
+                         __double2float_rn(hi.x), __double2float_rn(hi.y));
+}
+}  // namespace
+
+const float4 *bore_f32(const so3g_pixelization *pz, int mode, const double *bore, int n_time,
+                       cudaStream_t stream) {
+    const int kind = pix_kind(pz);
+    if (mode != SO3G_POINTING_MIXED || pz->coord_sys != SO3G_COORD_CAR ||
+        (kind != PX_FLAT_NT_NN && kind != PX_FLAT_T_NN) || n_time <= 0 || !bore)
+        return nullptr;
+    float4 *p = nullptr;
+    if (cudaMallocAsync(reinterpret_cast<void **>(&p), sizeof(float4) * (size_t)n_time,
+                        stream) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    k_bore_f32<<<(n_time + kBlock - 1) / kBlock, kBlock, 0, stream>>>(bore, p, n_time);
+    if (after_launch("boresight float32 copy") != SO3G_OK) {
+        cudaFreeAsync(p, stream);
+        clear_error();
+        return nullptr;
+    }
+    return p;
+}
+
+void bore_f32_free(const float4 *p, cudaStream_t stream) {
+    if (p) cudaFreeAsync(const_cast<float4 *>(p), stream);
+}
+
 int pix_kind(const so3g_pixelization *pz) {
     if (pz->pix_sys == SO3G_PIX_HEALPIX) return pz->tiled ? PX_HP_T : PX_HP_NT;
     return (pz->tiled ? 2 : 0) + (pz->interp == SO3G_INTERP_BILINEAR ? 1 : 0);
@@ -271,6 +307,15 @@ int so3g_init(void) {
         return set_error(SO3G_ERR_CUDA, "cudaMemcpy: %s", cudaGetErrorString(e));
     }
     g_fast_lut[dev] = f;
+    // Keep freed stream-ordered allocations (the boresight copies of the
+    // mixed pointing) in this process's pool instead of returning them to
+    // the driver at every synchronisation.
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        unsigned long long keep = 1ULL << 30;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    cudaGetLastError();
     return SO3G_OK;
 }
 

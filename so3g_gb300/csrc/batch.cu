@@ -127,6 +127,7 @@ int batch_entry(const so3g_pixelization *pz, const so3g_obs *obs, int32_t n_obs,
     L.a.ft = device_fast_tables();
     L.a.fc = make_fast_const(L.a.g);
     L.a.mc = make_mixed_const(L.a.g);
+    L.a.bore32 = nullptr;   // per-observation boresights: converted in the kernel
     L.a.fast = fast_mode(pz, L.a.ft);
     L.obs = obs;
     L.n_obs = n_obs;

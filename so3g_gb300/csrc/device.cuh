@@ -495,7 +495,7 @@ __device__ __forceinline__ void record_pixel_range(int *err, int tile, int det, 
 // float -> double by integer operations: exact, and no float64-pipe
 // instruction (GB300 runs float<->double conversions on its slow float64
 // pipe, at ~0.7 per clock per SM).
-__device__ __forceinline__ double f2d(float f) {
+static __device__ __noinline__ double f2d_special(float f) {
     const unsigned u = __float_as_uint(f);
     const unsigned s = u & 0x80000000u, ef = (u >> 23) & 0xffu, m = u & 0x7fffffu;
     // Subnormal floats: normalise the mantissa (leading one at bit p).
@@ -514,6 +514,19 @@ __device__ __forceinline__ double f2d(float f) {
     }
     const unsigned hw = s | (ed << 20) | (mant >> 3), lw = mant << 29;
     return __hiloint2double((int)hw, (int)lw);
+}
+
+// float -> double with integer instructions only; normal floats take the
+// short path (rebias the exponent, move the significand), zeros keep their
+// sign, and subnormals, infinities and NaNs go through f2d_special.
+__device__ __forceinline__ double f2d(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned a = u & 0x7fffffffu;
+    if (a - 0x00800000u < 0x7f000000u)
+        return __hiloint2double((int)((u & 0x80000000u) | ((a >> 3) + (896u << 20))),
+                                (int)(u << 29));
+    if (a == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+    return f2d_special(f);
 }
 
 // Compensated float32 addition (Knuth's TwoSum): s + e == a + b exactly.

@@ -30,6 +30,7 @@ struct GatherArgs {
     FastTables ft;
     FastConst fc;
     MixedConst mc;
+    const float4 *bore32;   // float32 boresight (mixed pointing), or NULL
 };
 
 // Adds the sample's map terms to its signal (src/Projection.cxx:1763-1765).
@@ -56,7 +57,7 @@ __device__ __forceinline__ void gather_taps(const GatherArgs &a, float *sp, int 
 }
 
 template <int C, int P>
-__device__ void exact_gather(const GatherArgs &a, int det, int t, const QuatD &ofs, float T,
+__device__ __noinline__ void exact_gather(const GatherArgs &a, int det, int t, const QuatD &ofs, float T,
                              float Pr) {
     constexpr int NT = PixTraits<P>::taps;
     double coords[4];
@@ -73,7 +74,7 @@ __device__ void exact_gather(const GatherArgs &a, int det, int t, const QuatD &o
 // float32 roundings of each term; false (signal untouched) when anything is
 // not certain.
 template <int C, int P>
-__device__ bool df_gather(const GatherArgs &a, int det, int t, const dfl (&qd)[4], float T,
+__device__ __forceinline__ bool df_gather(const GatherArgs &a, int det, int t, const dfl (&qd)[4], float T,
                           float Pr) {
     constexpr int NT = PixTraits<P>::taps;
     const double *bp = a.bore + 4LL * t;
@@ -152,11 +153,8 @@ __global__ void __launch_bounds__(kBlock, 5) k_from_map(GatherArgs a) {
         bool push = false, push_df = false;
         if (kMixedOK && mixed) {
             if (t < t1) {
-                const double *bp = a.bore + 4LL * t;
-                const double2 lo = __ldg(reinterpret_cast<const double2 *>(bp));
-                const double2 hi = __ldg(reinterpret_cast<const double2 *>(bp) + 1);
-                const float qb[4] = {d2f_trunc(lo.x), d2f_trunc(lo.y), d2f_trunc(hi.x),
-                                     d2f_trunc(hi.y)};
+                float qb[4];
+                load_bore_f32(a.bore32, a.bore, t, qb);
                 int pix[3];
                 float pf[3];
                 bool on = false;
@@ -290,5 +288,8 @@ extern "C" int so3g_proj_from_map(const so3g_pixelization *pz, const double *bor
     L.a.fast = fast_mode(pz, L.a.ft);
     L.grid = dim3((unsigned)n_det, (unsigned)((n_time + L.a.piece - 1) / L.a.piece));
     L.stream = (cudaStream_t)stream;
-    return dispatch_cp(pz->coord_sys, pix_kind(pz), L);
+    L.a.bore32 = bore_f32(pz, L.a.fast, boresight, n_time, L.stream);
+    rc = dispatch_cp(pz->coord_sys, pix_kind(pz), L);
+    bore_f32_free(L.a.bore32, L.stream);
+    return rc;
 }

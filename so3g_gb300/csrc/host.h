@@ -35,6 +35,13 @@ MixedConst make_mixed_const(const DGeom &g);
 // The pointing mode a kernel runs for a pixelization (0 exact, 1 certified,
 // 2 mixed): the exact path when the double-float tables are missing.
 int fast_mode(const so3g_pixelization *pz, const FastTables &ft);
+// Float32 copy of a boresight (n_time quaternions, rounded to nearest) for
+// the mixed pointing, in stream-ordered device memory; NULL when the
+// pixelization does not use it or the allocation fails (the kernels then
+// convert the float64 boresight themselves).  Release with bore_f32_free.
+const float4 *bore_f32(const so3g_pixelization *pz, int mode, const double *bore,
+                       int n_time, cudaStream_t stream);
+void bore_f32_free(const float4 *p, cudaStream_t stream);
 // Adds the map's tile table to the geometry; checks the tile count.
 int attach_map(const so3g_pixelization *pz, const so3g_map *m, DGeom *g);
 // Pixelizor kind (PX_*) of a pixelization.

@@ -67,6 +67,39 @@ __device__ __forceinline__ float d2f_trunc(double x) {
     return (ex > 896u && ex < 1151u) ? v : 0.f;
 }
 
+// A float64 value rounded to float32 (half-way cases away from zero) with
+// integer operations: relative error <= u.  A carry out of the significand
+// moves into the exponent, which is the correct rounding.  0 outside
+// [2^-126, 2^127).
+__device__ __forceinline__ float d2f_round(double x) {
+    const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
+    const unsigned ex = (hw >> 20) & 0x7ffu;
+    const unsigned mag = (((ex - 896u) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29)) +
+                         ((lw >> 28) & 1u);
+    const float v = __uint_as_float((hw & 0x80000000u) | mag);
+    return (ex > 896u && ex < 1150u) ? v : 0.f;
+}
+
+// The float32 boresight quaternion of sample t: from the float32 copy
+// when there is one, else rounded from the float64 boresight.
+__device__ __forceinline__ void load_bore_f32(const float4 *b32, const double *bore, int t,
+                                              float (&qb)[4]) {
+    if (b32) {
+        const float4 v = __ldg(b32 + t);
+        qb[0] = v.x;
+        qb[1] = v.y;
+        qb[2] = v.z;
+        qb[3] = v.w;
+    } else {
+        const double2 lo = __ldg(reinterpret_cast<const double2 *>(bore + 4LL * t));
+        const double2 hi = __ldg(reinterpret_cast<const double2 *>(bore + 4LL * t) + 1);
+        qb[0] = d2f_round(lo.x);
+        qb[1] = d2f_round(lo.y);
+        qb[2] = d2f_round(hi.x);
+        qb[3] = d2f_round(hi.y);
+    }
+}
+
 // Piecewise-linear table value in float32: knot i and fraction f of
 // u * (n-1); also returns the local slope (table units per unit of u).
 __device__ __forceinline__ float lut_f(const float4 *t, float u, float &slope) {
@@ -88,45 +121,52 @@ __device__ __forceinline__ bool mixed_car(const DGeom &g, const FastTables &ft,
                                           const MixedConst &mc, const float (&qb)[4],
                                           const float (&qd)[4], int nc, float T, float Pr,
                                           int *pix, bool &on, float *pf) {
-    // q = qb * qd.  Inputs: qb truncated (2u), qd rounded (u); each
-    // component is a 4-term dot product with sum |terms| <= |qb||qd| = 1:
-    // error <= (3u input + 4u rounding) = 7u; 8u is used.
+    // q = qb * qd with qb and qd rounded to float32 (relative u each).  The
+    // error quaternion dq = q~ - q has |dq| <= 2u (inputs: the product of
+    // quaternions multiplies norms) + 8u (four roundings per component,
+    // each <= u * sum|terms| <= u) = 10u.  A rotation off by dq points
+    // <= 2|dq| away, so the exact longitude of q~ is off by <= 20u / cos(lat)
+    // and sin(lat) by <= 20u cos(lat); |q~|^2 = 1 +- 20u scales sin(lat).
     const float a = fmaf(qb[0], qd[0], fmaf(-qb[1], qd[1], fmaf(-qb[2], qd[2], -qb[3] * qd[3])));
     const float b = fmaf(qb[0], qd[1], fmaf(qb[1], qd[0], fmaf(qb[2], qd[3], -qb[3] * qd[2])));
     const float c = fmaf(qb[0], qd[2], fmaf(-qb[1], qd[3], fmaf(qb[2], qd[0], qb[3] * qd[1])));
     const float d = fmaf(qb[0], qd[3], fmaf(qb[1], qd[2], fmaf(-qb[2], qd[1], qb[3] * qd[0])));
-    // cos(theta) = sin(lat): error <= 2 * 8u * (|a|+|b|+|c|+|d|) + 4u <= 36u.
+    // cos(theta) = sin(lat): error <= 20u (cos + |sin|) + 4u (roundings)
+    // <= 33u.
     const float cos_t = fmaf(a, a, fmaf(-b, b, fmaf(-c, c, d * d)));
     if (!(fabsf(cos_t) < 0.9f)) return false;
-    // lat = ASIN(cos_t): error <= slope * (36u + u) + 6u (table values and
+    // lat = ASIN(cos_t): error <= slope * (33u + u) + 5u (table values and
     // the final fma rounded to float32).
     float slope_lat;
     float lat = lut_f(ft.asin_t, fabsf(cos_t), slope_lat);
     if (cos_t < 0.f) lat = -lat;
-    // lon = ATAN2(Y, X), Y = c*d - a*b, X = c*a + d*b: |dY|, |dX| <= 18u.
+    // lon = ATAN2(Y, X), Y = c*d - a*b, X = c*a + d*b, |(X, Y)| = cos(lat)/2.
+    // Their float32 roundings are <= u each (|ca| + |db| <= 1/2), i.e. an
+    // angle <= 2.83u / cos(lat).
     const float Y = fmaf(c, d, -a * b), X = fmaf(c, a, d * b);
     const float ay = fabsf(Y), ax = fabsf(X);
     if (X < 0.f && !(ay > 64.f * kU)) return false;   // the +-pi seam
     const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
     const float inv_mx = __frcp_rn(mx);
-    // r = mn / mx: error <= 36u / mx + 2u; atan has slope <= 1.
+    // r = mn * (1/mx) rounded twice (2u); atan has slope <= 1.
     float slope_lon;
     float th = lut_f(ft.atan2_t, mn * inv_mx, slope_lon);
     float lon = (ax < ay) ? mc.half_pi - th : th;
     if (X < 0.f) lon = mc.pi - lon;
     if (Y < 0.f) lon = -lon;
-    // lon error <= 36u/mx + 6u (table) + 10u (the subtractions from pi/2
-    // and pi, and the float32 rounding of those constants); 20u is used.
-    const float elon = fmaf(36.f * kU, inv_mx, 20.f * kU);
-    const float elat = fmaf(37.f * kU, slope_lat, 6.f * kU);
+    // lon error <= 22.9u / cos(lat) + 2u (r) + 5.4u (table) + 9.5u (the
+    // subtractions from pi/2 and pi and those constants' roundings), and
+    // 1 / cos(lat) <= 1 / (2 mx): <= 11.5u / mx + 17u.
+    const float elon = fmaf(11.5f * kU, inv_mx, 17.f * kU);
+    const float elat = fmaf(34.f * kU, slope_lat, 5.f * kU);
     // Pixel coordinates x = lon / cdx + crpix_x - 1 + 0.5 (and y), with the
-    // float32 rounding of 1/cdx, the offset and the fma; x2 safety.
+    // float32 rounding of 1/cdx, of the offset and of the fma; x1.5 safety.
     const float lx = lon * mc.inv_cdx, ly = lat * mc.inv_cdy;
     const float x = fmaf(lon, mc.inv_cdx, mc.off_x), y = fmaf(lat, mc.inv_cdy, mc.off_y);
-    const float ex = 2.f * fmaf(fabsf(mc.inv_cdx), elon,
-                                kU * (2.f * fabsf(lx) + fabsf(mc.off_x) + fabsf(x)));
-    const float ey = 2.f * fmaf(fabsf(mc.inv_cdy), elat,
-                                kU * (2.f * fabsf(ly) + fabsf(mc.off_y) + fabsf(y)));
+    const float ex = 1.5f * fmaf(fabsf(mc.inv_cdx), elon,
+                                 kU * (fabsf(lx) + fabsf(mc.off_x) + fabsf(x)));
+    const float ey = 1.5f * fmaf(fabsf(mc.inv_cdy), elat,
+                                 kU * (fabsf(ly) + fabsf(mc.off_y) + fabsf(y)));
     const float fx = floorf(x), fy = floorf(y);
     const float rx = x - fx, ry = y - fy;
     if (!(rx > ex && rx < 1.f - ex && ry > ey && ry < 1.f - ey)) return false;

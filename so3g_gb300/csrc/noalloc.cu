@@ -174,6 +174,7 @@ extern "C" int so3g_proj_to_map_noalloc(
         L.a.err = derr;
         L.a.map = map_data;
         L.a.fast = 0;  // exact pointing: the double-float knots are not in the scratch
+        L.a.bore32 = nullptr;
         L.grid = dim3((unsigned)n_work, (unsigned)((max_len + L.a.piece - 1) / L.a.piece));
         L.stream = st;
         rc = dispatch_cp(pz->coord_sys, pix_kind(pz), L);

@@ -67,7 +67,10 @@ int scatter_entry(const so3g_pixelization *pz, const double *bore, int32_t n_tim
     L.a.fast = fast_mode(pz, L.a.ft);
     L.grid = dim3((unsigned)n_seg, (unsigned)((max_len + L.a.piece - 1) / L.a.piece));
     L.stream = (cudaStream_t)stream;
-    return dispatch_cp(pz->coord_sys, pix_kind(pz), L);
+    L.a.bore32 = bore_f32(pz, L.a.fast, bore, n_time, L.stream);
+    rc = dispatch_cp(pz->coord_sys, pix_kind(pz), L);
+    bore_f32_free(L.a.bore32, L.stream);
+    return rc;
 }
 
 }  // namespace

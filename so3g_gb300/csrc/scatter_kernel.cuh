@@ -47,6 +47,7 @@ struct ScatterArgs {
     FastTables ft;
     FastConst fc;
     MixedConst mc;
+    const float4 *bore32;   // float32 boresight (mixed pointing), or NULL
 };
 
 
@@ -92,8 +93,10 @@ __device__ __forceinline__ void tap_values(float sig, const float *pf, float w, 
 }
 
 // One sample through the exact float64 pointing, added with plain atomics.
+// Not inlined: it runs for few, compacted samples, and inlined its float64
+// registers would weigh on the main loop.
 template <int C, int P, bool WEIGHT>
-__device__ void exact_sample(const ScatterArgs &a, int det, int t, const QuatD &ofs, float T,
+__device__ __noinline__ void exact_sample(const ScatterArgs &a, int det, int t, const QuatD &ofs, float T,
                              float Pr, float det_wt, const int *mult, unsigned vmask) {
     constexpr int NT = PixTraits<P>::taps;
     constexpr int NV = WEIGHT ? 6 : 3;
@@ -123,7 +126,7 @@ __device__ void exact_sample(const ScatterArgs &a, int det, int t, const QuatD &
 // One sample through the certified double-float pointing, added with plain
 // atomics; false (nothing added) when it is not certified.
 template <int C, int P, bool WEIGHT>
-__device__ bool df_sample(const ScatterArgs &a, int det, int t, const dfl (&qd)[4], float T,
+__device__ __forceinline__ bool df_sample(const ScatterArgs &a, int det, int t, const dfl (&qd)[4], float T,
                           float Pr, float det_wt, const int *mult, unsigned vmask) {
     constexpr int NT = PixTraits<P>::taps;
     constexpr int NV = WEIGHT ? 6 : 3;
@@ -233,11 +236,8 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
         if (live) {
             bool done = false;
             if (kMixedOK && mixed) {
-                const double *bp = a.bore + 4LL * t;
-                const double2 lo = __ldg(reinterpret_cast<const double2 *>(bp));
-                const double2 hi = __ldg(reinterpret_cast<const double2 *>(bp) + 1);
-                const float qb[4] = {d2f_trunc(lo.x), d2f_trunc(lo.y), d2f_trunc(hi.x),
-                                     d2f_trunc(hi.y)};
+                float qb[4];
+                load_bore_f32(a.bore32, a.bore, t, qb);
                 bool on = false;
                 if (mixed_car<P>(a.g, a.ft, a.mc, qb, qd32, nc, T, Pr, pix[0], on, pf)) {
                     n = on ? 1 : 0;
@@ -269,7 +269,8 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
             }
             if (!WEIGHT && n > 0) sig = __ldg(a.signal + det * a.sig_stride + t);
         }
-        if (kFastOK && fast) qn = warp_enqueue(wq, qn, push, t);
+        // (Mixed pointing fills the exact queue from the double-float pass.)
+        if (kFastOK && fast && !mixed) qn = warp_enqueue(wq, qn, push, t);
         if (kMixedOK && mixed) qdf = warp_enqueue(wdf, qdf, push_df, t);
 #pragma unroll
         for (int k = 0; k < NT; k++) {
