@@ -31,7 +31,18 @@ struct GatherArgs {
     FastConst fc;
     MixedConst mc;
     const float4 *bore32;   // float32 boresight (mixed pointing), or NULL
+    const float4 *map32;    // float32 (T, Q, U, 0) per pixel (mixed, untiled), or NULL
 };
+
+// The untiled map's components as float32, pixel by pixel (one 16-byte
+// load per sample in the mixed from_map).
+__global__ void k_map_f32(const double *map, int nc, long long npix, float4 *out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npix) return;
+    float v[3] = {0.f, 0.f, 0.f};
+    for (int c = 0; c < nc; c++) v[c] = __double2float_rn(__ldg(map + c * npix + i));
+    out[i] = make_float4(v[0], v[1], v[2], 0.f);
+}
 
 // Adds the sample's map terms to its signal (src/Projection.cxx:1763-1765).
 template <int P, int NT>
@@ -168,10 +179,18 @@ __global__ void __launch_bounds__(kBlock, 5) k_from_map(GatherArgs a) {
                             // float32 terms (the mixed-precision contract).
                             float *sp = a.signal + det * a.sig_stride + t;
                             float s = *sp;
+                            if (a.map32) {
+                                const float4 m = __ldg(a.map32 + off);
+                                s = fmaf(m.x, pf[0], s);
+                                if (nc > 1) s = fmaf(m.y, pf[1], s);
+                                if (nc > 2) s = fmaf(m.z, pf[2], s);
+                            } else {
 #pragma unroll
-                            for (int c = 0; c < 3; c++)
-                                if (c < nc)
-                                    s = fmaf(d2f_trunc(__ldg(a.map + off + c * plane)), pf[c], s);
+                                for (int c = 0; c < 3; c++)
+                                    if (c < nc)
+                                        s = fmaf(d2f_round(__ldg(a.map + off + c * plane)), pf[c],
+                                                 s);
+                            }
                             *sp = s;
                         }
                     }
@@ -289,7 +308,28 @@ extern "C" int so3g_proj_from_map(const so3g_pixelization *pz, const double *bor
     L.grid = dim3((unsigned)n_det, (unsigned)((n_time + L.a.piece - 1) / L.a.piece));
     L.stream = (cudaStream_t)stream;
     L.a.bore32 = bore_f32(pz, L.a.fast, boresight, n_time, L.stream);
+    // Mixed pointing on an untiled map: a float32 copy of the map, read with
+    // one 16-byte load per sample.
+    float4 *map32 = nullptr;
+    if (L.a.bore32 && !pz->tiled) {
+        const long long npix = (long long)L.a.g.ny * L.a.g.nx;
+        if (cudaMallocAsync(reinterpret_cast<void **>(&map32), sizeof(float4) * (size_t)npix,
+                            L.stream) == cudaSuccess) {
+            k_map_f32<<<(unsigned)((npix + kBlock - 1) / kBlock), kBlock, 0, L.stream>>>(
+                map->data, pz->n_comp, npix, map32);
+            if (after_launch("map float32 copy") != SO3G_OK) {
+                cudaFreeAsync(map32, L.stream);
+                map32 = nullptr;
+                clear_error();
+            }
+        } else {
+            cudaGetLastError();
+            map32 = nullptr;
+        }
+    }
+    L.a.map32 = map32;
     rc = dispatch_cp(pz->coord_sys, pix_kind(pz), L);
+    if (map32) cudaFreeAsync(map32, L.stream);
     bore_f32_free(L.a.bore32, L.stream);
     return rc;
 }
