@@ -80,6 +80,8 @@ def parse():
     ap.add_argument("--tiled", action="store_true", help="cfg3: the Tiled NEST variant")
     ap.add_argument("--pointing", default="mixed", choices=["mixed", "certified", "exact"],
                     help="pointing mode of the timed steps")
+    ap.add_argument("--precomp", action="store_true",
+                    help="time the Precomp engine on the workload's precomputed pointing")
     return ap.parse_args()
 
 
@@ -457,6 +459,87 @@ def run_e2e(args, c, eng, q, dets, resp, sig_dev, dev):
 
 
 # ---------------------------------------------------------------------------
+# Precomputed pointing: ProjEng_Precomp on the workload's pointing matrix.
+
+def run_precomp(args, c):
+    """One step = Precomp to_map + from_map over all samples, the pixel
+    indices and spin factors computed once beforehand (pointing_matrix)."""
+    import torch
+    import so3g_gb300
+    from so3g_gb300 import _abi
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    lib = _abi.lib()
+    p, q, dets, resp = host_inputs(c)
+    eng = p.get_ProjEng("TQU")
+    q_d, dets_d, resp_d = (torch.from_numpy(x).to(dev) for x in (q, dets, resp))
+    pix, spin = eng.pointing_matrix(q_d, dets_d, resp_d)
+    del q_d
+    sig = make_signal(torch, c, dev)
+    pc = so3g_gb300.ProjEng_Precomp_NonTiled()
+    m = torch.zeros((3,) + tuple(c["shape"]), dtype=torch.float64, device=dev)
+    out = torch.zeros_like(sig)
+    stream = torch.cuda.current_stream()
+    N = c["n_det"] * c["n_time"]
+
+    def step(ev):
+        m.zero_()
+        ev[0].record(stream)
+        pc.to_map(m, pix, spin, sig)
+        ev[1].record(stream)
+        out.zero_()
+        ev[2].record(stream)
+        pc.from_map(m, pix, spin, out)
+        ev[3].record(stream)
+
+    for _ in range(args.warmup):
+        step([torch.cuda.Event(enable_timing=True) for _ in range(4)])
+    torch.cuda.synchronize()
+    n0 = lib.so3g_launch_count()
+    evs = []
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            step(ev)
+            evs.append(ev)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    launches = lib.so3g_launch_count() - n0
+    ms = e0.elapsed_time(e1) / args.steps
+    tm = float(np.mean([a.elapsed_time(b) for a, b, _, _ in evs]))
+    fm = float(np.mean([a.elapsed_time(b) for _, _, a, b in evs]))
+    npix = c["shape"][0] * c["shape"][1]
+    # Compulsory bytes per sample: pixel (2 int32) + spin (3 float32) +
+    # signal (4, read; from_map also writes it) + the map once.
+    b_tm = 8. + 12. + 4. + 16. * 3 * npix / N
+    b_fm = 8. + 12. + 8. + 8. * 3 * npix / N
+    hbm, kind = peaks()
+    ach_tm = b_tm * N / (tm * 1e-3) / 1e9
+    ach_fm = b_fm * N / (fm * 1e-3) / 1e9
+    metric, workload, map_shape = describe(c)
+    line = {"metric": "Precomp to_map/from_map TOD samples/s (CAR TQU, precomputed pointing)",
+            "value": N / (ms * 1e-3), "unit": "samples/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": workload + ", pointing precomputed (ProjEng_Precomp)",
+                       "n_det": c["n_det"], "n_time": c["n_time"], "map": map_shape,
+                       "step": "Precomp to_map + from_map",
+                       "l2": "inputs larger than L2 (pointing + TOD %.1f GB)" % (N * 24 / 1e9),
+                       "parallelism": "single GPU"},
+            "op_ms": {"to_map": tm, "from_map": fm},
+            "roofline": {"bound": "hbm", "kernel": "precomp from_map", "achieved": ach_fm,
+                         "peak": hbm, "unit": "GB/s", "frac": ach_fm / hbm, "traffic": None,
+                         "bytes_per_sample": b_fm, "peak_kind": kind,
+                         "to_map": {"achieved": ach_tm, "frac": ach_tm / hbm,
+                                    "bytes_per_sample": b_tm}},
+            "clocks": clk.summary(), "gpu_launches": int(launches)}
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
 # Batched map-making input: many observations into one map.
 
 def batch_inputs(c, scale=1.0, seed=0):
@@ -674,6 +757,8 @@ def main():
     if args.config == "cfg4" and args.impl == "ours":
         return run_batch(args, dict(CONFIGS["cfg4"]))
     c = config(args)
+    if args.precomp and args.impl == "ours":
+        return run_precomp(args, c)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:

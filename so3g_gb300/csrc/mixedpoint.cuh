@@ -131,12 +131,15 @@ __device__ __forceinline__ bool mixed_car(const DGeom &g, const FastTables &ft,
     const float b = fmaf(qb[0], qd[1], fmaf(qb[1], qd[0], fmaf(qb[2], qd[3], -qb[3] * qd[2])));
     const float c = fmaf(qb[0], qd[2], fmaf(-qb[1], qd[3], fmaf(qb[2], qd[0], qb[3] * qd[1])));
     const float d = fmaf(qb[0], qd[3], fmaf(qb[1], qd[2], fmaf(-qb[2], qd[1], qb[3] * qd[0])));
-    // cos(theta) = sin(lat): error <= 20u (cos + |sin|) + 4u (roundings)
-    // <= 33u.
+    // cos(theta) = sin(lat): error <= 20u cos(lat) (rotation) + 20u |sin(lat)|
+    // (norm) + 4u (roundings).
     const float cos_t = fmaf(a, a, fmaf(-b, b, fmaf(-c, c, d * d)));
     if (!(fabsf(cos_t) < 0.9f)) return false;
-    // lat = ASIN(cos_t): error <= slope * (33u + u) + 5u (table values and
-    // the final fma rounded to float32).
+    // lat = ASIN(cos_t): the table's slope times that error, plus u |cos_t|
+    // (the index) and 5u (table values and the final fma rounded to
+    // float32).  The rotation part times the slope is <= 20.1u (the secant
+    // slope of asin on a knot interval is within 1.0003 of 1 / cos(lat) for
+    // |sin lat| < 0.9): <= 25.1u + slope (21u |cos_t| + 4u).
     float slope_lat;
     float lat = lut_f(ft.asin_t, fabsf(cos_t), slope_lat);
     if (cos_t < 0.f) lat = -lat;
@@ -158,7 +161,7 @@ __device__ __forceinline__ bool mixed_car(const DGeom &g, const FastTables &ft,
     // subtractions from pi/2 and pi and those constants' roundings), and
     // 1 / cos(lat) <= 1 / (2 mx): <= 11.5u / mx + 17u.
     const float elon = fmaf(11.5f * kU, inv_mx, 17.f * kU);
-    const float elat = fmaf(34.f * kU, slope_lat, 5.f * kU);
+    const float elat = fmaf(slope_lat, fmaf(21.f * kU, fabsf(cos_t), 4.f * kU), 25.1f * kU);
     // Pixel coordinates x = lon / cdx + crpix_x - 1 + 0.5 (and y), with the
     // float32 rounding of 1/cdx, of the offset and of the fma; x1.5 safety.
     const float lx = lon * mc.inv_cdx, ly = lat * mc.inv_cdy;
