@@ -574,6 +574,7 @@ def run_batch(args, c):
     lib = _abi.lib()
     p, hobs = batch_inputs(c, args.batch_scale)
     eng = p.get_ProjEng("TQU")
+    eng.pointing = POINTING[args.pointing]
     g = torch.Generator(device=dev)
     g.manual_seed(0)
     obs = []
@@ -647,6 +648,7 @@ def run_batch(args, c):
                        "3x%dx%d float64 map" % (ny, nx),
            "n_obs": len(obs), "samples": N, "sizes": sizes, "batch_scale": args.batch_scale,
            "step": "to_map + to_weight_map, one CUDA graph with the tuned launches",
+           "pointing": args.pointing,
            "l2": "inputs larger than L2 (TOD %.1f GB)" % (N * 4 / 1e9),
            "parallelism": "single GPU"}
     line = {"metric": "batched to_map + to_weight_map TOD samples/s (CAR TQU, 16 obs)",
@@ -773,8 +775,9 @@ def main():
            "map": map_shape, "step": step_name,
            "l2": "inputs larger than L2 (TOD %.1f GB)" % (c["n_det"] * c["n_time"] * 4 / 1e9),
            "precision": PRECISION[args.pointing] + (
-               "" if c["kind"] == "car" or args.pointing != "mixed" else
-               " (mixed applies to CAR nearest neighbour; this pixelization runs certified)"),
+               "" if c["kind"] in ("car", "hp") or args.pointing != "mixed" else
+               " (mixed applies to CAR nearest neighbour and HEALPix; this pixelization "
+               "runs certified)"),
            "pointing": args.pointing,
            "parallelism": "replicas" if world > 1 else "single GPU"}
 

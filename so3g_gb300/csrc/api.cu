@@ -151,7 +151,9 @@ const float4 *bore_f32(const so3g_pixelization *pz, int mode, const double *bore
                        cudaStream_t stream) {
     const int kind = pix_kind(pz);
     if (mode != SO3G_POINTING_MIXED || pz->coord_sys != SO3G_COORD_CAR ||
-        (kind != PX_FLAT_NT_NN && kind != PX_FLAT_T_NN) || n_time <= 0 || !bore)
+        (kind != PX_FLAT_NT_NN && kind != PX_FLAT_T_NN && kind != PX_HP_NT &&
+         kind != PX_HP_T) ||
+        n_time <= 0 || !bore)
         return nullptr;
     float4 *p = nullptr;
     if (cudaMallocAsync(reinterpret_cast<void **>(&p), sizeof(float4) * (size_t)n_time,

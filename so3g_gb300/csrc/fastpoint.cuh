@@ -154,6 +154,14 @@ __device__ __forceinline__ bool df_split(double x, dfl &out) {
 }
 
 
+// Double-float of a float64: integer operations (df_split) where they
+// apply, the conversion instructions otherwise.
+__device__ __forceinline__ dfl df_of(double x) {
+    dfl r;
+    if (df_split(x, r)) return r;
+    return df_from_double(x);
+}
+
 // The integer part of a double-float and the remaining fraction (exact).
 __device__ __forceinline__ int df_floor(dfl x, dfl &frac) {
     float f = floorf(x.hi);

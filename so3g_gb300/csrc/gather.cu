@@ -138,15 +138,14 @@ __global__ void __launch_bounds__(kBlock, 5) k_from_map(GatherArgs a) {
         for (int t = t0 + threadIdx.x; t < t1; t += blockDim.x) exact_gather<C, P>(a, det, t, ofs, T, Pr);
         return;
     }
-    dfl qd[4] = {df_from_double(ofs.a), df_from_double(ofs.b), df_from_double(ofs.c),
-                 df_from_double(ofs.d)};
+    dfl qd[4] = {df_of(ofs.a), df_of(ofs.b), df_of(ofs.c), df_of(ofs.d)};
     constexpr bool mixed = kMixedOK;
     float qd32[4];
     if (kMixedOK && mixed) {
-        qd32[0] = __double2float_rn(ofs.a);
-        qd32[1] = __double2float_rn(ofs.b);
-        qd32[2] = __double2float_rn(ofs.c);
-        qd32[3] = __double2float_rn(ofs.d);
+        qd32[0] = d2f_round(ofs.a);
+        qd32[1] = d2f_round(ofs.b);
+        qd32[2] = d2f_round(ofs.c);
+        qd32[3] = d2f_round(ofs.d);
     }
     int *wq = s_queue + (threadIdx.x >> 5) * kWarpQueue;
     int *wdf = s_queue + ((kBlock >> 5) + (threadIdx.x >> 5)) * kWarpQueue;
@@ -169,7 +168,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_from_map(GatherArgs a) {
                 int pix[3];
                 float pf[3];
                 bool on = false;
-                if (mixed_car<P>(a.g, a.ft, a.mc, qb, qd32, nc, T, Pr, pix, on, pf)) {
+                if (mixed_pointing<P>(a.g, a.ft, a.mc, qb, qd32, nc, T, Pr, pix, on, pf)) {
                     if (on) {
                         long long off, plane;
                         const int bad = locate<P>(a.g, pix, &off, &plane);
@@ -299,7 +298,7 @@ extern "C" int so3g_proj_from_map(const so3g_pixelization *pz, const double *bor
     L.a.signal = signal;
     L.a.sig_stride = sig_det_stride;
     L.a.segs = Segs{nullptr, n_time};
-    L.a.piece = piece_len(n_time);
+    L.a.piece = piece_len(n_time, n_det);
     L.a.err = err;
     L.a.ft = device_fast_tables();
     L.a.fc = make_fast_const(L.a.g);
@@ -312,7 +311,9 @@ extern "C" int so3g_proj_from_map(const so3g_pixelization *pz, const double *bor
     // one 16-byte load per sample.
     float4 *map32 = nullptr;
     if (L.a.bore32 && !pz->tiled) {
-        const long long npix = (long long)L.a.g.ny * L.a.g.nx;
+        const long long npix = pz->pix_sys == SO3G_PIX_HEALPIX
+                                   ? L.a.g.npix
+                                   : (long long)L.a.g.ny * L.a.g.nx;
         if (cudaMallocAsync(reinterpret_cast<void **>(&map32), sizeof(float4) * (size_t)npix,
                             L.stream) == cudaSuccess) {
             k_map_f32<<<(unsigned)((npix + kBlock - 1) / kBlock), kBlock, 0, L.stream>>>(

@@ -51,9 +51,14 @@ int pix_kind(const so3g_pixelization *pz);
 constexpr int kBlock = 256;
 constexpr int kMinPiece = 4096;
 
-// Piece length so that no segment needs more than 65535 pieces.
-inline int piece_len(long long max_len) {
+// Piece length for n_seg segments of up to max_len samples: at least
+// kMinPiece, doubled (up to 32768) while the grid would keep over 16 waves
+// of resident blocks (fewer pieces amortise the per-piece set-up), and as
+// far as needed to keep a segment within 65535 pieces.
+inline int piece_len(long long max_len, long long n_seg = 1) {
+    constexpr long long kManyBlocks = 16LL * 152 * 5;
     long long p = kMinPiece;
+    while (p < 32768 && n_seg * ((max_len + 2 * p - 1) / (2 * p)) >= kManyBlocks) p *= 2;
     while ((max_len + p - 1) / p > 65535) p *= 2;
     return (int)p;
 }

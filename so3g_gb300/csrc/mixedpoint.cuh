@@ -1,5 +1,6 @@
 // mixedpoint.cuh -- float32 pointing with certified pixel indices
-// (SO3G_POINTING_MIXED), for CAR with a nearest-neighbour flat pixelizor.
+// (SO3G_POINTING_MIXED), for CAR with a nearest-neighbour flat pixelizor
+// and for HEALPix.
 //
 // The sample's quaternion product, table lookups, pixel coordinates and
 // spin factors are evaluated in plain float32.  Alongside, a bound on the
@@ -36,8 +37,10 @@ struct FastEligible {
 template <int C, int P>
 struct MixedEligible {
     static constexpr bool value =
-        C == SO3G_COORD_CAR && (P == PX_FLAT_NT_NN || P == PX_FLAT_T_NN);
+        C == SO3G_COORD_CAR &&
+        (P == PX_FLAT_NT_NN || P == PX_FLAT_T_NN || P == PX_HP_NT || P == PX_HP_T);
 };
+
 
 struct MixedConst {
     float inv_cdx, inv_cdy;   // 1/cdelt, rounded to float32
@@ -112,15 +115,21 @@ __device__ __forceinline__ float lut_f(const float4 *t, float u, float &slope) {
     return fmaf(k.z, f, k.x);
 }
 
-// The float32 tier.  Returns false when the sample must go to the
-// double-float path: near the native poles (|sin lat| >= 0.9, where the
-// float32 spin factors lose accuracy), at the atan2 seam, or when a pixel
-// coordinate is within its error bound of an integer.
-template <int P>
-__device__ __forceinline__ bool mixed_car(const DGeom &g, const FastTables &ft,
-                                          const MixedConst &mc, const float (&qb)[4],
-                                          const float (&qd)[4], int nc, float T, float Pr,
-                                          int *pix, bool &on, float *pf) {
+// The float32 quaternion product and CAR longitude/latitude of a sample,
+// with bounds on their errors against the reference's float64 values.
+// False where the float32 tier does not apply: near the native poles
+// (|sin lat| >= 0.9, where the float32 spin factors lose accuracy) and at
+// the atan2 seam.
+struct MixedLonLat {
+    float a, b, c, d;      // q = qb * qd
+    float cos_t;           // sin(lat)
+    float lon, lat;
+    float elon, elat;      // error bounds (no safety factor)
+};
+
+__device__ __forceinline__ bool mixed_lonlat(const FastTables &ft, const MixedConst &mc,
+                                             const float (&qb)[4], const float (&qd)[4],
+                                             MixedLonLat &o) {
     // q = qb * qd with qb and qd rounded to float32 (relative u each).  The
     // error quaternion dq = q~ - q has |dq| <= 2u (inputs: the product of
     // quaternions multiplies norms) + 8u (four roundings per component,
@@ -153,27 +162,78 @@ __device__ __forceinline__ bool mixed_car(const DGeom &g, const FastTables &ft,
     const float inv_mx = __frcp_rn(mx);
     // r = mn * (1/mx) rounded twice (2u); atan has slope <= 1.
     float slope_lon;
-    float th = lut_f(ft.atan2_t, mn * inv_mx, slope_lon);
+    const float th = lut_f(ft.atan2_t, mn * inv_mx, slope_lon);
     float lon = (ax < ay) ? mc.half_pi - th : th;
     if (X < 0.f) lon = mc.pi - lon;
     if (Y < 0.f) lon = -lon;
     // lon error <= 22.9u / cos(lat) + 2u (r) + 5.4u (table) + 9.5u (the
     // subtractions from pi/2 and pi and those constants' roundings), and
     // 1 / cos(lat) <= 1 / (2 mx): <= 11.5u / mx + 17u.
-    const float elon = fmaf(11.5f * kU, inv_mx, 17.f * kU);
-    const float elat = fmaf(slope_lat, fmaf(21.f * kU, fabsf(cos_t), 4.f * kU), 25.1f * kU);
+    o.a = a;
+    o.b = b;
+    o.c = c;
+    o.d = d;
+    o.cos_t = cos_t;
+    o.lon = lon;
+    o.lat = lat;
+    o.elon = fmaf(11.5f * kU, inv_mx, 17.f * kU);
+    o.elat = fmaf(slope_lat, fmaf(21.f * kU, fabsf(cos_t), 4.f * kU), 25.1f * kU);
+    return true;
+}
+
+// Spin factors (:1180-1209) in float32 with c = Nc/h, s = Ns/h, h^2 = D =
+// (a^2 + d^2)(b^2 + c^2) (= (1 - cos^2)/4 without cancellation).
+__device__ __forceinline__ void mixed_spin(const MixedLonLat &o, int nc, float T, float Pr,
+                                           float *pf) {
+    if (nc == 1) {
+        pf[0] = T;
+        pf[1] = pf[2] = 0.f;
+        return;
+    }
+    const float a = o.a, b = o.b, c = o.c, d = o.d;
+    const float Nc = fmaf(a, c, -b * d), Ns = fmaf(c, d, a * b);
+    const float D = fmaf(a, a, d * d) * fmaf(b, b, c * c);
+    const float k = Pr * __frcp_rn(D);
+    const float v1 = fmaf(Nc, Nc, -Ns * Ns) * k, v2 = 2.f * Nc * Ns * k;
+    if (nc == 2) {
+        pf[0] = v1;
+        pf[1] = v2;
+        pf[2] = 0.f;
+    } else {
+        pf[0] = T;
+        pf[1] = v1;
+        pf[2] = v2;
+    }
+}
+
+// Floor of a float32 value whose error bound is e; false when the value is
+// within e of an integer (then the reference's floor is not certain).
+__device__ __forceinline__ bool floor_cert(float v, float e, int &i) {
+    const float f = floorf(v);
+    const float r = v - f;
+    i = (int)f;
+    return r > e && r < 1.f - e;
+}
+
+// The float32 tier for CAR with a nearest-neighbour flat pixelizor.
+// Returns false when the sample must go to the double-float path.
+template <int P>
+__device__ __forceinline__ bool mixed_car(const DGeom &g, const FastTables &ft,
+                                          const MixedConst &mc, const float (&qb)[4],
+                                          const float (&qd)[4], int nc, float T, float Pr,
+                                          int *pix, bool &on, float *pf) {
+    MixedLonLat o;
+    if (!mixed_lonlat(ft, mc, qb, qd, o)) return false;
     // Pixel coordinates x = lon / cdx + crpix_x - 1 + 0.5 (and y), with the
     // float32 rounding of 1/cdx, of the offset and of the fma; x1.5 safety.
-    const float lx = lon * mc.inv_cdx, ly = lat * mc.inv_cdy;
-    const float x = fmaf(lon, mc.inv_cdx, mc.off_x), y = fmaf(lat, mc.inv_cdy, mc.off_y);
-    const float ex = 1.5f * fmaf(fabsf(mc.inv_cdx), elon,
+    const float lx = o.lon * mc.inv_cdx, ly = o.lat * mc.inv_cdy;
+    const float x = fmaf(o.lon, mc.inv_cdx, mc.off_x), y = fmaf(o.lat, mc.inv_cdy, mc.off_y);
+    const float ex = 1.5f * fmaf(fabsf(mc.inv_cdx), o.elon,
                                  kU * (fabsf(lx) + fabsf(mc.off_x) + fabsf(x)));
-    const float ey = 1.5f * fmaf(fabsf(mc.inv_cdy), elat,
+    const float ey = 1.5f * fmaf(fabsf(mc.inv_cdy), o.elat,
                                  kU * (fabsf(ly) + fabsf(mc.off_y) + fabsf(y)));
-    const float fx = floorf(x), fy = floorf(y);
-    const float rx = x - fx, ry = y - fy;
-    if (!(rx > ex && rx < 1.f - ex && ry > ey && ry < 1.f - ey)) return false;
-    const int ix = (int)fx, iy = (int)fy;
+    int ix, iy;
+    if (!(floor_cert(x, ex, ix) & floor_cert(y, ey, iy))) return false;
     if (P == PX_FLAT_NT_NN) {
         on = ix >= 0 && ix < g.nx && iy >= 0 && iy < g.ny;
         if (on) {
@@ -190,28 +250,121 @@ __device__ __forceinline__ bool mixed_car(const DGeom &g, const FastTables &ft,
             pix[2] = tx - sub_x * g.tx;
         }
     }
-    if (!on) return true;
-    // Spin factors (:1180-1209) with c = Nc/h, s = Ns/h, h^2 = D
-    // = (a^2 + d^2)(b^2 + c^2) (= (1 - cos^2)/4 without cancellation).
-    if (nc == 1) {
-        pf[0] = T;
-        pf[1] = pf[2] = 0.f;
-        return true;
-    }
-    const float Nc = fmaf(a, c, -b * d), Ns = fmaf(c, d, a * b);
-    const float D = fmaf(a, a, d * d) * fmaf(b, b, c * c);
-    const float k = Pr * __frcp_rn(D);
-    const float v1 = fmaf(Nc, Nc, -Ns * Ns) * k, v2 = 2.f * Nc * Ns * k;
-    if (nc == 2) {
-        pf[0] = v1;
-        pf[1] = v2;
-        pf[2] = 0.f;
-    } else {
-        pf[0] = T;
-        pf[1] = v1;
-        pf[2] = v2;
-    }
+    if (on) mixed_spin(o, nc, T, Pr, pf);
     return true;
+}
+
+// The float32 tier for HEALPix (Pixelizor_Healpix::GetPixels through
+// ang2pix, src/healpix_bare.c:46-78, 271-306): z = sin(lat) and s =
+// cos(lat) from __sincosf of the float32 latitude (absolute error
+// <= 2^-21.41 for |lat| <= pi), every integer decision certified against
+// the propagated error bound (x1.5 safety).  Returns false when the sample
+// must go to the double-float path; the pixel is always on the map.
+template <int P>
+__device__ __forceinline__ bool mixed_healpix(const DGeom &g, const FastTables &ft,
+                                              const MixedConst &mc, const float (&qb)[4],
+                                              const float (&qd)[4], int nc, float T, float Pr,
+                                              int *pix, float *pf) {
+    const long long nside = g.nside;
+    if (nside > (1LL << 20)) return false;
+    MixedLonLat o;
+    if (!mixed_lonlat(ft, mc, qb, qd, o)) return false;
+    constexpr float m = 1.5f;
+    float z, s;
+    __sincosf(o.lat, &z, &s);
+    const float ez = fmaf(fabsf(s), o.elat, 3.8e-7f);
+    const float es = fmaf(fabsf(z), o.elat, 3.8e-7f);
+    // x = phi / (2 pi), wrapped into [0, 1); tt = 4 x.
+    constexpr float kInv2Pi = 0.15915494f;
+    float x = o.lon * kInv2Pi;
+    float ex = fmaf(o.elon, kInv2Pi, 2.f * kU * fabsf(x));
+    if (!(fabsf(x) > m * ex)) return false;
+    if (x < 0.f) {
+        x += 1.f;
+        ex += kU;
+    }
+    const float tt = 4.f * x, ett = 4.f * ex;
+    const float za = fabsf(z);
+    const float fn = (float)nside;
+    // za <= 2/3 (the float32 2/3 is within 2e-8 of the float64 constant).
+    if (!(fabsf(za - 0.6666667f) > fmaf(m, ez, 3e-8f))) return false;
+    int f, ix, iy;
+    if (za < 0.6666667f) {
+        // Equatorial belt: jp = 0.5 + tt - 0.75 z, jm = 0.5 + tt + 0.75 z;
+        // ix, iy, the face from floor(jm * nside), floor(jp * nside).
+        const float t1 = 0.5f + tt, t2 = 0.75f * z;
+        const float jp = t1 - t2, jm = t1 + t2;
+        const float ej =
+            fmaf(m, fmaf(0.75f, ez, ett), kU * (fabsf(t1) + 1.f + fabsf(jp) + fabsf(jm)));
+        const float JP = jp * fn, JM = jm * fn;
+        const float eJ = fmaf(ej, fn, kU * fmaxf(fabsf(JP), fabsf(JM)));
+        int Jp, Jm;
+        if (!(floor_cert(JP, eJ, Jp) & floor_cert(JM, eJ, Jm))) return false;
+        if (Jp < 0 || Jm < 0) return false;
+        const int ns = (int)nside;
+        const int ifp = Jp / ns, ifm = Jm / ns;
+        ix = Jm - ifm * ns;
+        iy = (1 + ifp) * ns - Jp - 1;
+        f = (ifp == ifm) ? (ifp | 4) : ((ifp < ifm) ? ifp : (ifm + 8));
+    } else {
+        // Polar caps: tmp = s / sqrt((1 + za) / 3), jp = tp tmp, jm = (1 - tp) tmp.
+        int ntt;
+        if (!floor_cert(tt, m * ett, ntt)) return false;
+        if (ntt >= 4) ntt = 3;
+        const float tp = tt - (float)ntt;
+        const float q = (1.f + za) * 0.33333334f;
+        const float eq = fmaf(ez, 0.33333334f, 3.f * kU * q);
+        const float sq = sqrtf(q);
+        const float tmp = s / sq;
+        const float etmp = fmaf(es + tmp * eq / (2.f * q), 1.f / sq, 3.f * kU * tmp);
+        const float jp = tp * tmp, jm = (1.f - tp) * tmp;
+        const float ejp = m * fmaf(ett, tmp, fmaf(tp, etmp, kU * jp));
+        const float ejm = m * fmaf(ett, tmp, fmaf(1.f - tp, etmp, 2.f * kU * jm));
+        // The clamps at 1 only act within rounding of za = 2/3.
+        if (!(jp < 1.f - ejp && jm < 1.f - ejm)) return false;
+        float hx, hy, ehx, ehy;
+        if (z > 0.f) {
+            hx = 1.f - jm;
+            hy = 1.f - jp;
+            ehx = ejm + kU;
+            ehy = ejp + kU;
+            f = ntt;
+        } else {
+            hx = jp;
+            hy = jm;
+            ehx = ejp;
+            ehy = ejm;
+            f = ntt + 8;
+        }
+        const float HX = hx * fn, HY = hy * fn;
+        if (!(floor_cert(HX, fmaf(ehx, fn, kU * fabsf(HX)), ix) &
+              floor_cert(HY, fmaf(ehy, fn, kU * fabsf(HY)), iy)))
+            return false;
+    }
+    const long long ip = hp_hpd2pix(nside, P == PX_HP_T ? true : (g.nest != 0), f, ix, iy);
+    if (ip < 0 || ip >= g.npix) return false;
+    if (P == PX_HP_NT) {
+        pix[0] = (int)ip;
+    } else {
+        pix[0] = (int)(ip / g.nppt);
+        pix[1] = (int)(ip % g.nppt);
+    }
+    mixed_spin(o, nc, T, Pr, pf);
+    return true;
+}
+
+// The float32 tier of one sample for pixelization P: one tap (weight 1)
+// when `on`.  False hands the sample to the double-float path.
+template <int P>
+__device__ __forceinline__ bool mixed_pointing(const DGeom &g, const FastTables &ft,
+                                               const MixedConst &mc, const float (&qb)[4],
+                                               const float (&qd)[4], int nc, float T, float Pr,
+                                               int *pix, bool &on, float *pf) {
+    if (P == PX_HP_NT || P == PX_HP_T) {
+        on = true;
+        return mixed_healpix<P>(g, ft, mc, qb, qd, nc, T, Pr, pix, pf);
+    }
+    return mixed_car<P>(g, ft, mc, qb, qd, nc, T, Pr, pix, on, pf);
 }
 
 }  // namespace so3g

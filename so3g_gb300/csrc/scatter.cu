@@ -57,7 +57,7 @@ int scatter_entry(const so3g_pixelization *pz, const double *bore, int32_t n_tim
     L.a.sig_stride = sig_det_stride;
     L.a.det_weights = det_weights;
     L.a.segs = Segs{ranges ? ranges->seg : nullptr, n_time};
-    L.a.piece = piece_len(max_len);
+    L.a.piece = piece_len(max_len, n_seg);
     L.a.accum = accum;
     L.a.err = err;
     L.a.map = map->data;

@@ -204,16 +204,16 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
     int *wdf = s_queue + ((kBlock >> 5) + (threadIdx.x >> 5)) * kWarpQueue;
     int qn = 0, qdf = 0;
     if (kFastOK && fast) {
-        qd[0] = df_from_double(ofs.a);
-        qd[1] = df_from_double(ofs.b);
-        qd[2] = df_from_double(ofs.c);
-        qd[3] = df_from_double(ofs.d);
+        qd[0] = df_of(ofs.a);
+        qd[1] = df_of(ofs.b);
+        qd[2] = df_of(ofs.c);
+        qd[3] = df_of(ofs.d);
     }
     if (kMixedOK && mixed) {
-        qd32[0] = __double2float_rn(ofs.a);
-        qd32[1] = __double2float_rn(ofs.b);
-        qd32[2] = __double2float_rn(ofs.c);
-        qd32[3] = __double2float_rn(ofs.d);
+        qd32[0] = d2f_round(ofs.a);
+        qd32[1] = d2f_round(ofs.b);
+        qd32[2] = d2f_round(ofs.c);
+        qd32[3] = d2f_round(ofs.d);
     }
     // Recomputes the exact-path queue with the float64 pointing.
     auto drain_exact = [&]() {
@@ -239,7 +239,7 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
                 float qb[4];
                 load_bore_f32(a.bore32, a.bore, t, qb);
                 bool on = false;
-                if (mixed_car<P>(a.g, a.ft, a.mc, qb, qd32, nc, T, Pr, pix[0], on, pf)) {
+                if (mixed_pointing<P>(a.g, a.ft, a.mc, qb, qd32, nc, T, Pr, pix[0], on, pf)) {
                     n = on ? 1 : 0;
                     w[0] = 1.f;
                 } else {

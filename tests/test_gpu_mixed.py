@@ -108,3 +108,62 @@ def test_mixed_maps_within_tolerance(tiled):
         out[mode] = [flat(x) for x in (m, w, back)]
     for a, b in zip(out[_abi.POINTING_EXACT], out[_abi.POINTING_MIXED]):
         assert np.abs(a - b).max() <= 1e-6 * np.abs(a).max()
+
+
+def _probe_hp(eng, q, dets, resp, tiled):
+    import torch
+    from test_gpu_certified import _hp_probe_maps
+    qd, dd, rd = (torch.from_numpy(x).cuda() for x in (q, dets, resp))
+    maps = _hp_probe_maps(eng, tiled, 3)
+    out = {}
+    for mode in MODES:
+        eng.pointing = mode
+        out[mode] = [eng.from_map(m, qd, dd, rd, None).cpu().numpy() for m in maps]
+    ex, mx = out[_abi.POINTING_EXACT], out[_abi.POINTING_MIXED]
+    assert bits_equal(ex[0], mx[0])
+    for a, b in zip(ex[1:], mx[1:]):
+        assert np.abs(a - b).max() <= 2e-5
+        assert np.abs(a - b).mean() <= 2e-7
+
+
+@pytest.mark.parametrize("nside,nest,tiled", [(64, False, False), (1024, False, False),
+                                              (1024, True, False), (512, True, True)])
+def test_mixed_healpix_at_scale(nside, nest, tiled):
+    from test_gpu_certified import _hp_engine
+    Q1, dets, resp, gamma, _ = synth.workload(100, 30_000, seed=61, radius_deg=2.0, el=40.,
+                                              throw=60., v_az=3.)
+    Q2, _, _, _, _ = synth.workload(100, 30_000, seed=61, radius_deg=2.0, el=62., az0=0.,
+                                    throw=60., v_az=3.)
+    p, eng = _hp_engine(nside, nest, tiled)
+    q = synth.native(p, np.concatenate([Q1, Q2]))
+    _probe_hp(eng, q, dets, resp, tiled)
+
+
+def test_mixed_healpix_edges():
+    """The belt/cap boundary, phi = 0 and +-pi, and in-face edges of the
+    equatorial belt (as in the certified tests)."""
+    from test_gpu_certified import _hp_engine
+    rng = np.random.default_rng(63)
+    nside = 256
+    n = 30000
+    z_edge = rng.choice([2 / 3, -2 / 3], n // 3) + rng.choice([0., 1e-15, -1e-7, 1e-6], n // 3)
+    lat_a, lon_a = np.arcsin(z_edge), rng.uniform(-np.pi, np.pi, n // 3)
+    lat_b = rng.uniform(-1.1, 1.1, n // 3)
+    lon_b = rng.choice([0., np.pi, -np.pi], n // 3) + rng.choice([0., 1e-9, -1e-7, 1e-6], n // 3)
+    k = n - 2 * (n // 3)
+    jp = rng.integers(1, 4 * nside, k) / nside
+    jm = jp + rng.integers(-nside // 2, nside // 2, k) / nside
+    z = (jm - jp) / 1.5
+    tt = (jp + jm) / 2 - 0.5
+    ok = np.abs(z) < 0.66
+    lat_c = np.arcsin(z[ok])
+    lon_c = tt[ok] / 4 * 2 * np.pi
+    lon_c = np.where(lon_c > np.pi, lon_c - 2 * np.pi, lon_c)
+    lat = np.concatenate([lat_a, lat_b, lat_c])
+    lon = np.concatenate([lon_a, lon_b, lon_c])
+    q = _quats_at(lon, lat, rng.uniform(0, np.pi, len(lat)))
+    dets = np.array([[1., 0., 0., 0.]])
+    resp = np.ones((1, 2), np.float32)
+    for nest in (False, True):
+        p, eng = _hp_engine(nside, nest, False)
+        _probe_hp(eng, q, dets, resp, False)
