@@ -544,14 +544,14 @@ constexpr int kDirectRuns = 4;
 // Sums the values of each run of equal keys across the warp (lanes in
 // order) and adds the run totals to map[key + mult[k] * plane] from the
 // run's first lane.  Keys < 0 are not flushed.  All 32 lanes must call.
-template <int NV>
+template <int NV, int DIRECT_RUNS = kDirectRuns>
 __device__ __forceinline__ void flush_runs(long long key, long long plane, float (&v)[NV],
                                            const int (&mult)[NV], unsigned vmask, double *map) {
     const int lane = threadIdx.x & 31;
     long long prev = __shfl_up_sync(kFull, key, 1);
     bool head = (lane == 0) || (key != prev);
     unsigned heads = __ballot_sync(kFull, head);
-    if (__popc(heads) >= kDirectRuns) {
+    if (__popc(heads) >= DIRECT_RUNS) {
         if (key >= 0) {
 #pragma unroll
             for (int k = 0; k < NV; k++)

@@ -104,24 +104,42 @@ __global__ void __launch_bounds__(kBlock) k_pc_scatter(PcArgs a) {
                 if (i < nc && j < nc) vmask |= 1u << k;
             }
     }
+    // The next round's pointing and signal are loaded before this round's
+    // atomics are issued, so that two rounds of loads are in flight.
+    int p[3] = {-1, 0, 0}, pn[3] = {-1, 0, 0};
+    float pf[3] = {0.f, 0.f, 0.f}, pfn[3] = {0.f, 0.f, 0.f};
+    float sg = 0.f, sgn = 0.f;
+    auto fetch = [&](int t, int *pp, float *ff, float &ss) {
+        if (t < t1) {
+            const long long s = (long long)det * a.n_time + t;
+            load_tuple<TILED>(a, s, pp);
+#pragma unroll
+            for (int c = 0; c < 3; c++)
+                if (c < nc) ff[c] = __ldg(a.spin + s * nc + c);
+            if (!WEIGHT) ss = __ldg(a.signal + det * a.sig_stride + t);
+        } else {
+            pp[0] = -1;
+        }
+    };
+    fetch(t0 + (threadIdx.x & ~31) + lane, pn, pfn, sgn);
     for (int base = t0 + (threadIdx.x & ~31); base < t1; base += blockDim.x) {
         const int t = base + lane;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            p[c] = pn[c];
+            pf[c] = pfn[c];
+        }
+        sg = sgn;
+        fetch(t + blockDim.x, pn, pfn, sgn);
         long long off = -1, plane = 0;
         float v[NV];
 #pragma unroll
         for (int k = 0; k < NV; k++) v[k] = 0.f;
         if (t < t1) {
-            const long long s = (long long)det * a.n_time + t;
-            int p[3];
-            load_tuple<TILED>(a, s, p);
             if (p[0] >= 0 && pc_locate<TILED>(a, p, det, t, &off, &plane)) {
-                float pf[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-                for (int c = 0; c < 3; c++)
-                    if (c < nc) pf[c] = __ldg(a.spin + s * nc + c);
                 if (!WEIGHT) {
                     // src/Projection.cxx:2117
-                    const float sig = __ldg(a.signal + det * a.sig_stride + t);
+                    const float sig = sg;
 #pragma unroll
                     for (int c = 0; c < 3; c++) v[c] = det_wt * sig * pf[c];
                 } else {
@@ -135,7 +153,9 @@ __global__ void __launch_bounds__(kBlock) k_pc_scatter(PcArgs a) {
             }
         }
         if (a.accum == SO3G_ACCUM_WARP_RUNS) {
-            flush_runs<NV>(off, plane, v, mult, vmask, a.map);
+            // Every run reduced in the warp (no direct atomics): this kernel
+            // has issue slots to spare, and fewer atomics reach L2.
+            flush_runs<NV, 33>(off, plane, v, mult, vmask, a.map);
         } else if (off >= 0) {
 #pragma unroll
             for (int k = 0; k < NV; k++)
@@ -157,13 +177,25 @@ __global__ void __launch_bounds__(kBlock) k_pc_from_map(PcArgs a) {
         if (p[0] < 0) continue;
         long long off, plane;
         if (!pc_locate<TILED>(a, p, det, t, &off, &plane)) continue;
-        float sig = 0;
+        // sig += pf * map, a float64 product and sum rounded to float32 per
+        // component: certified double-float roundings (fast_accum), the
+        // float64 arithmetic itself for a sample where one is uncertain.
+        float pf[3], sig = 0.f;
+        double mv[3];
+        bool ok = true;
 #pragma unroll
         for (int c = 0; c < 3; c++) {
             if (c < nc) {
-                const float pf = __ldg(a.spin + s * nc + c);
-                sig += pf * __ldg(a.map + off + c * plane);
+                pf[c] = __ldg(a.spin + s * nc + c);
+                mv[c] = __ldg(a.map + off + c * plane);
+                ok = ok && fast_accum(sig, mv[c], pf[c]);
             }
+        }
+        if (!ok) {
+            sig = 0.f;
+#pragma unroll
+            for (int c = 0; c < 3; c++)
+                if (c < nc) sig += pf[c] * mv[c];
         }
         a.signal_out[det * a.sig_stride + t] += sig;
     }
