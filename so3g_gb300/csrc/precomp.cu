@@ -153,9 +153,7 @@ __global__ void __launch_bounds__(kBlock) k_pc_scatter(PcArgs a) {
             }
         }
         if (a.accum == SO3G_ACCUM_WARP_RUNS) {
-            // Every run reduced in the warp (no direct atomics): this kernel
-            // has issue slots to spare, and fewer atomics reach L2.
-            flush_runs<NV, 33>(off, plane, v, mult, vmask, a.map);
+            flush_runs<NV>(off, plane, v, mult, vmask, a.map);
         } else if (off >= 0) {
 #pragma unroll
             for (int k = 0; k < NV; k++)
@@ -170,34 +168,48 @@ __global__ void __launch_bounds__(kBlock) k_pc_from_map(PcArgs a) {
     int det, t0, t1;
     if (!seg_piece(a.segs, a.piece, det, t0, t1)) return;
     const int nc = a.nc;
-    for (int t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
-        const long long s = (long long)det * a.n_time + t;
-        int p[3];
-        load_tuple<TILED>(a, s, p);
-        if (p[0] < 0) continue;
-        long long off, plane;
-        if (!pc_locate<TILED>(a, p, det, t, &off, &plane)) continue;
-        // sig += pf * map, a float64 product and sum rounded to float32 per
-        // component: certified double-float roundings (fast_accum), the
-        // float64 arithmetic itself for a sample where one is uncertain.
-        float pf[3], sig = 0.f;
-        double mv[3];
-        bool ok = true;
+    // Four samples per thread and iteration, their pointing loads issued
+    // together (more bytes in flight per thread).
+    constexpr int U = 4;
+    for (int tb = t0 + threadIdx.x; tb < t1; tb += U * blockDim.x) {
+        int pu[U][3];
 #pragma unroll
-        for (int c = 0; c < 3; c++) {
-            if (c < nc) {
-                pf[c] = __ldg(a.spin + s * nc + c);
-                mv[c] = __ldg(a.map + off + c * plane);
-                ok = ok && fast_accum(sig, mv[c], pf[c]);
+        for (int u = 0; u < U; u++) {
+            const int t = tb + u * blockDim.x;
+            pu[u][0] = -1;
+            if (t < t1) load_tuple<TILED>(a, (long long)det * a.n_time + t, pu[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int t = tb + u * blockDim.x;
+            if (t >= t1) break;
+            const long long s = (long long)det * a.n_time + t;
+            const int *p = pu[u];
+            if (p[0] < 0) continue;
+            long long off, plane;
+            if (!pc_locate<TILED>(a, p, det, t, &off, &plane)) continue;
+            // sig += pf * map, a float64 product and sum rounded to float32 per
+            // component: certified double-float roundings (fast_accum), the
+            // float64 arithmetic itself for a sample where one is uncertain.
+            float pf[3], sig = 0.f;
+            double mv[3];
+            bool ok = true;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                if (c < nc) {
+                    pf[c] = __ldg(a.spin + s * nc + c);
+                    mv[c] = __ldg(a.map + off + c * plane);
+                    ok = ok && fast_accum(sig, mv[c], pf[c]);
+                }
             }
-        }
-        if (!ok) {
-            sig = 0.f;
+            if (!ok) {
+                sig = 0.f;
 #pragma unroll
-            for (int c = 0; c < 3; c++)
-                if (c < nc) sig += pf[c] * mv[c];
+                for (int c = 0; c < 3; c++)
+                    if (c < nc) sig += pf[c] * mv[c];
+            }
+            a.signal_out[det * a.sig_stride + t] += sig;
         }
-        a.signal_out[det * a.sig_stride + t] += sig;
     }
 }
 
