@@ -18,6 +18,7 @@ __global__ void __launch_bounds__(kBlock, kScatterBlocksPerSM)
     k_scatter_batch(ScatterArgs base, const so3g_obs *obs, int n_obs,
                     const long long *work_off, long long n_work) {
     __shared__ int s_queue[QueueInts<C, P, MODE>::value];
+    __shared__ WarpPiece s_wp[kBlock / 32];
     for (long long w = blockIdx.x; w < n_work; w += gridDim.x) {
         // The observation holding item w: largest o with work_off[o] <= w.
         int lo = 0, hi = n_obs - 1;
@@ -45,7 +46,7 @@ __global__ void __launch_bounds__(kBlock, kScatterBlocksPerSM)
         a.signal = ob.signal;
         a.sig_stride = ob.sig_det_stride;
         a.det_weights = ob.det_weights;
-        scatter_piece<C, P, WEIGHT, MODE>(a, det, t0, t1, s_queue);
+        scatter_piece<C, P, WEIGHT, MODE>(a, det, t0, t1, s_queue, s_wp);
     }
 }
 

@@ -128,6 +128,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_from_map(GatherArgs a) {
     constexpr bool kFastOK = FastEligible<C, P>::value && MODE >= 1;
     constexpr bool kMixedOK = MixedEligible<C, P>::value && MODE == 2;
     __shared__ int s_queue[!kFastOK ? 1 : (kMixedOK ? 2 : 1) * (kBlock / 32) * kWarpQueue];
+    __shared__ WarpPiece s_wp[kFastOK ? kBlock / 32 : 1];
     int det, t0, t1;
     if (!seg_piece(a.segs, a.piece, det, t0, t1)) return;
     const QuatD ofs = load_quat(a.dets + 4LL * det);
@@ -150,10 +151,17 @@ __global__ void __launch_bounds__(kBlock, 5) k_from_map(GatherArgs a) {
     int *wq = s_queue + (threadIdx.x >> 5) * kWarpQueue;
     int *wdf = s_queue + ((kBlock >> 5) + (threadIdx.x >> 5)) * kWarpQueue;
     int qn = 0, qdf = 0;
+    WarpPiece *wp = s_wp + (threadIdx.x >> 5);
+    if ((threadIdx.x & 31) == 0) {
+        wp->ofs = ofs;
+#pragma unroll
+        for (int k = 0; k < 4; k++) wp->qd[k] = qd[k];
+    }
+    __syncwarp();
     auto drain_exact = [&]() {
         __syncwarp();
         for (int i = threadIdx.x & 31; i < qn; i += 32)
-            exact_gather<C, P>(a, det, wq[i], ofs, T, Pr);
+            exact_gather<C, P>(a, det, wq[i], wp->ofs, T, Pr);
         __syncwarp();
         qn = 0;
     };
@@ -203,7 +211,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_from_map(GatherArgs a) {
                 for (int base = 0; base < qdf; base += 32) {
                     const int i = base + (threadIdx.x & 31);
                     const int ts = i < qdf ? wdf[i] : 0;
-                    const bool px = i < qdf && !df_gather<C, P>(a, det, ts, qd, T, Pr);
+                    const bool px = i < qdf && !df_gather<C, P>(a, det, ts, wp->qd, T, Pr);
                     qn = warp_enqueue(wq, qn, px, ts);
                     if (qn > kWarpQueue - 32) drain_exact();
                 }

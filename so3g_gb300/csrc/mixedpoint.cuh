@@ -42,6 +42,13 @@ struct MixedEligible {
 };
 
 
+// Per-warp copy, in shared memory, of the detector quantities only the
+// fallback passes use: kept out of the main loop's registers.
+struct WarpPiece {
+    QuatD ofs;      // detector offset (exact path)
+    dfl qd[4];      // its double-float split (double-float path)
+};
+
 struct MixedConst {
     float inv_cdx, inv_cdy;   // 1/cdelt, rounded to float32
     float off_x, off_y;       // crpix - 1 + 0.5

@@ -75,20 +75,23 @@ __device__ __forceinline__ unsigned value_slots(int nc, int *mult) {
     return vmask;
 }
 
-template <bool WEIGHT, int NV>
+// UNIT_W: a nearest-neighbour tap, whose weight is exactly 1 (the
+// multiplications by it are exact and are left out).
+template <bool WEIGHT, int NV, bool UNIT_W = false>
 __device__ __forceinline__ void tap_values(float sig, const float *pf, float w, float det_wt,
                                            float (&v)[NV]) {
     if (!WEIGHT) {
         // src/Projection.cxx:1807 -- float32 product, left to right
 #pragma unroll
-        for (int c = 0; c < 3; c++) v[c] = sig * pf[c] * w * det_wt;
+        for (int c = 0; c < 3; c++) v[c] = UNIT_W ? sig * pf[c] * det_wt : sig * pf[c] * w * det_wt;
     } else {
         // src/Projection.cxx:1850
         int s = 0;
 #pragma unroll
         for (int i = 0; i < 3; i++)
 #pragma unroll
-            for (int j = i; j < 3; j++, s++) v[s] = pf[i] * pf[j] * w * w * det_wt;
+            for (int j = i; j < 3; j++, s++)
+                v[s] = UNIT_W ? pf[i] * pf[j] * det_wt : pf[i] * pf[j] * w * w * det_wt;
     }
 }
 
@@ -181,7 +184,7 @@ struct QueueInts {
 // (QueueInts<C, P, MODE> ints).
 template <int C, int P, bool WEIGHT, int MODE>
 __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int t0, int t1,
-                                              int *s_queue) {
+                                              int *s_queue, WarpPiece *s_wp) {
     constexpr bool kFastOK = PointingVariant<C, P, MODE>::fast;
     float det_wt = 1.f;
     if (a.det_weights) {
@@ -203,11 +206,19 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
     int *wq = s_queue + (threadIdx.x >> 5) * kWarpQueue;
     int *wdf = s_queue + ((kBlock >> 5) + (threadIdx.x >> 5)) * kWarpQueue;
     int qn = 0, qdf = 0;
+    WarpPiece *wp = s_wp + (threadIdx.x >> 5);
     if (kFastOK && fast) {
         qd[0] = df_of(ofs.a);
         qd[1] = df_of(ofs.b);
         qd[2] = df_of(ofs.c);
         qd[3] = df_of(ofs.d);
+        __syncwarp();
+        if ((threadIdx.x & 31) == 0) {
+            wp->ofs = ofs;
+#pragma unroll
+            for (int k = 0; k < 4; k++) wp->qd[k] = qd[k];
+        }
+        __syncwarp();
     }
     if (kMixedOK && mixed) {
         qd32[0] = d2f_round(ofs.a);
@@ -219,7 +230,7 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
     auto drain_exact = [&]() {
         __syncwarp();
         for (int i = threadIdx.x & 31; i < qn; i += 32)
-            exact_sample<C, P, WEIGHT>(a, det, wq[i], ofs, T, Pr, det_wt, mult, vmask);
+            exact_sample<C, P, WEIGHT>(a, det, wq[i], wp->ofs, T, Pr, det_wt, mult, vmask);
         __syncwarp();
         qn = 0;
     };
@@ -284,7 +295,7 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
                     record_missing_tile(a.err, bad);
                     off = -1;
                 } else {
-                    tap_values<WEIGHT>(sig, pf, w[k], det_wt, v);
+                    tap_values<WEIGHT, NV, NT == 1>(sig, pf, w[k], det_wt, v);
                 }
             }
             if (NT > 1 && !__any_sync(kFull, off >= 0)) continue;
@@ -305,8 +316,8 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
                 const int i = base + (threadIdx.x & 31);
                 const int ts = i < qdf ? wdf[i] : 0;
                 const bool px =
-                    i < qdf && !df_sample<C, P, WEIGHT>(a, det, ts, qd, T, Pr, det_wt, mult,
-                                                        vmask);
+                    i < qdf && !df_sample<C, P, WEIGHT>(a, det, ts, wp->qd, T, Pr, det_wt,
+                                                        mult, vmask);
                 qn = warp_enqueue(wq, qn, px, ts);
                 if (qn > kWarpQueue - 32) drain_exact();
             }
@@ -320,9 +331,10 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
 template <int C, int P, bool WEIGHT, int MODE>
 __global__ void __launch_bounds__(kBlock, kScatterBlocksPerSM) k_scatter(ScatterArgs a) {
     __shared__ int s_queue[QueueInts<C, P, MODE>::value];
+    __shared__ WarpPiece s_wp[kBlock / 32];
     int det, t0, t1;
     if (!seg_piece(a.segs, a.piece, det, t0, t1)) return;
-    scatter_piece<C, P, WEIGHT, MODE>(a, det, t0, t1, s_queue);
+    scatter_piece<C, P, WEIGHT, MODE>(a, det, t0, t1, s_queue, s_wp);
 }
 
 
