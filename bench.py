@@ -121,6 +121,23 @@ def npix_of(c):
     return 12 * c["nside"] ** 2 if c["kind"] == "hp" else c["shape"][0] * c["shape"][1]
 
 
+def max_over_ranks(ms, device=None):
+    """The slowest rank's step time (ms): every rank runs an independent
+    replica, so the job's step ends when the last replica's does."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return ms
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(samples_per_rank, world, ms):
+    """Whole-job samples/s: every rank's samples over the slowest step."""
+    return samples_per_rank * world / (ms * 1e-3)
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -366,10 +383,7 @@ def run_ours(args, c, rank, world):
     mode = POINTING[args.pointing]
     ms, op_ms, launches, clocks = timed(_abi.ACCUM_WARP_RUNS, args.steps, args.warmup,
                                         pointing=mode)
-    if world > 1:
-        t = torch.tensor([ms], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dev)
     res = {"ms_per_step": ms, "op_ms": op_ms, "launches": launches, "clocks": clocks}
     if world == 1 and c["kind"] != "zea_grad" and mode != _abi.POINTING_CERTIFIED:
         # The bit-exact certified mode, for comparison.
@@ -805,7 +819,7 @@ def main():
         return
     hbm, kind = peaks()
     ms = res["ms_per_step"]
-    value = N * world / (ms * 1e-3)
+    value = replica_throughput(N, world, ms)
     op = "to_map" if "to_map" in res["op_ms"] else list(res["op_ms"])[0]
     B = algorithmic_bytes(c, op)
     achieved = B * N / (res["op_ms"][op] * 1e-3) / 1e9

@@ -152,10 +152,11 @@ __device__ __forceinline__ bool mixed_lonlat(const FastTables &ft, const MixedCo
     const float cos_t = fmaf(a, a, fmaf(-b, b, fmaf(-c, c, d * d)));
     if (!(fabsf(cos_t) < 0.9f)) return false;
     // lat = ASIN(cos_t): the table's slope times that error, plus u |cos_t|
-    // (the index) and 5u (table values and the final fma rounded to
-    // float32).  The rotation part times the slope is <= 20.1u (the secant
-    // slope of asin on a knot interval is within 1.0003 of 1 / cos(lat) for
-    // |sin lat| < 0.9): <= 25.1u + slope (21u |cos_t| + 4u).
+    // (the index) and the table's roundings (2u |lat| + 0.01u, as for the
+    // longitude).  The rotation part times the slope is <= 20.1u (the
+    // secant slope of asin on a knot interval is within 1.0003 of
+    // 1 / cos(lat) for |sin lat| < 0.9): <= 20.11u + 2u |lat|
+    // + slope (21u |cos_t| + 4u).
     float slope_lat;
     float lat = lut_f(ft.asin_t, fabsf(cos_t), slope_lat);
     if (cos_t < 0.f) lat = -lat;
@@ -173,9 +174,11 @@ __device__ __forceinline__ bool mixed_lonlat(const FastTables &ft, const MixedCo
     float lon = (ax < ay) ? mc.half_pi - th : th;
     if (X < 0.f) lon = mc.pi - lon;
     if (Y < 0.f) lon = -lon;
-    // lon error <= 22.9u / cos(lat) + 2u (r) + 5.4u (table) + 9.5u (the
-    // subtractions from pi/2 and pi and those constants' roundings), and
-    // 1 / cos(lat) <= 1 / (2 mx): <= 11.5u / mx + 17u.
+    // lon error <= 22.9u / cos(lat) + 2u (r) + the table's roundings
+    // (u |th| + u |dv f| + u |th|, with |dv f| <= 1e-4: 2u |th| + 0.01u)
+    // + 3.2u if th was subtracted from pi/2 + 6.3u if from pi (those
+    // constants' roundings and the subtractions'), and 1 / cos(lat) <=
+    // 1 / (2 mx).
     o.a = a;
     o.b = b;
     o.c = c;
@@ -183,8 +186,10 @@ __device__ __forceinline__ bool mixed_lonlat(const FastTables &ft, const MixedCo
     o.cos_t = cos_t;
     o.lon = lon;
     o.lat = lat;
-    o.elon = fmaf(11.5f * kU, inv_mx, 17.f * kU);
-    o.elat = fmaf(slope_lat, fmaf(21.f * kU, fabsf(cos_t), 4.f * kU), 25.1f * kU);
+    o.elon = fmaf(11.5f * kU, inv_mx,
+                  fmaf(2.f * kU, th, (2.01f + (ax < ay ? 3.2f : 0.f) + (X < 0.f ? 6.3f : 0.f)) * kU));
+    o.elat = fmaf(slope_lat, fmaf(21.f * kU, fabsf(cos_t), 4.f * kU),
+                  fmaf(2.f * kU, fabsf(lat), 20.11f * kU));
     return true;
 }
 
