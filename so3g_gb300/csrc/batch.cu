@@ -14,7 +14,7 @@ namespace so3g {
 namespace {
 
 template <int C, int P, bool WEIGHT, int MODE>
-__global__ void __launch_bounds__(kBlock, kScatterBlocksPerSM)
+__global__ void __launch_bounds__(kBlock, MODE == 2 ? kMixedBlocksPerSM : kScatterBlocksPerSM)
     k_scatter_batch(ScatterArgs base, const so3g_obs *obs, int n_obs,
                     const long long *work_off, long long n_work) {
     __shared__ int s_queue[QueueInts<C, P, MODE>::value];

@@ -121,10 +121,11 @@ __device__ __forceinline__ bool df_gather(const GatherArgs &a, int det, int t, c
     return ok;
 }
 
-// Compiled for 5 resident blocks per SM (at most 51 registers), one
-// variant per pointing mode (0 exact, 1 certified, 2 mixed).
+// Compiled for 5 resident blocks per SM (at most 51 registers; mixed
+// pointing: 7), one variant per pointing mode (0 exact, 1 certified, 2
+// mixed).
 template <int C, int P, int MODE>
-__global__ void __launch_bounds__(kBlock, 5) k_from_map(GatherArgs a) {
+__global__ void __launch_bounds__(kBlock, MODE == 2 ? 7 : 5) k_from_map(GatherArgs a) {
     constexpr bool kFastOK = FastEligible<C, P>::value && MODE >= 1;
     constexpr bool kMixedOK = MixedEligible<C, P>::value && MODE == 2;
     __shared__ int s_queue[!kFastOK ? 1 : (kMixedOK ? 2 : 1) * (kBlock / 32) * kWarpQueue];
