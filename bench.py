@@ -211,7 +211,7 @@ def make_signal(torch, c, dev, seed=0):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons, sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons, sampled every 50 ms."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -225,7 +225,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -267,12 +267,17 @@ class ClockSampler:
 
 
 # DRAM bytes per sample (dram__bytes_read.sum + dram__bytes_write.sum / samples)
-# of one ncu capture of the certified to_map and from_map kernels, CAR TQU
-# 3x2000x2000, 200 det x 1M samples (profiles/to_map_from_map_certified_
-# car_tqu_200det_1M.md).  The traffic is the signal (4 B read, from_map also
-# 4 B written) plus the boresight per detector, so it scales with the samples.
-MEASURED_TRAFFIC_PER_SAMPLE = {"to_map": (834.33e6 + 3.78e6) / 2e8,
-                               "from_map": (835.40e6 + 747.14e6) / 2e8}
+# of one ncu capture of the to_map and from_map kernels, CAR TQU 3x2000x2000,
+# 200 det x 1M samples, per pointing mode (profiles/to_map_from_map_*_car_
+# tqu_200det_1M.md).  The traffic is the signal (4 B read, from_map also 4 B
+# written), the boresight per detector and (mixed to_map) spilled registers,
+# so it scales with the samples.
+MEASURED_TRAFFIC_PER_SAMPLE = {
+    "certified": {"to_map": (834.33e6 + 3.78e6) / 2e8,
+                  "from_map": (835.40e6 + 747.14e6) / 2e8},
+    "mixed": {"to_map": (907.08e6 + 125.03e6) / 2e8,
+              "from_map": (894.75e6 + 860.11e6) / 2e8},
+}
 
 
 def algorithmic_bytes(c, op):
@@ -830,8 +835,9 @@ def main():
             "op_ms": res["op_ms"],
             "roofline": {"bound": "hbm", "kernel": op, "achieved": achieved, "peak": hbm,
                          "unit": "GB/s", "frac": achieved / hbm,
-                         "traffic": (MEASURED_TRAFFIC_PER_SAMPLE[op] * N
-                                     if c["kind"] == "car" and op in MEASURED_TRAFFIC_PER_SAMPLE
+                         "traffic": (MEASURED_TRAFFIC_PER_SAMPLE[args.pointing][op] * N
+                                     if c["kind"] == "car" and op in
+                                     MEASURED_TRAFFIC_PER_SAMPLE.get(args.pointing, {})
                                      else None),
                          "bytes_per_sample": B, "peak_kind": kind},
             "clocks": res["clocks"], "gpu_launches": int(res["launches"])}

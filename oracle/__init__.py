@@ -3,8 +3,9 @@
 A ctypes wrapper around oracle/proj_oracle.cpp, the operation-by-operation
 restatement of the reference arithmetic (so3g src/Projection.cxx,
 include/so_linterp.h, src/healpix_bare.c).  Only the tests, the smoke
-check of __graft_entry__ and the CPU-baseline leg of bench.py use it, as
-the checker or the timed CPU baseline; the so3g_gb300 package never does.
+check of __graft_entry__ and the CPU-baseline leg of bench.py use it, to
+check results or as the timed CPU baseline; the so3g_gb300 package never
+does.
 
 Parity pin: the oracle's trig tables and HEALPix ang2pix are checked
 against golden vectors generated from the reference's own so_linterp.h and

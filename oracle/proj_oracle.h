@@ -6,8 +6,8 @@
  * Pixelizor2_Flat, Pixelizor_Healpix, spin_proj_factors, to_map,
  * to_weight_map, from_map, ProjEng_Precomp), include/so_linterp.h and the
  * HEALPix ang2pix routines of src/healpix_bare.c.  It is used by the tests
- * to check the CUDA library, by __graft_entry__.smoke() as the checker and
- * by bench.py as the timed CPU baseline.  The product never links or calls
+ * to check the CUDA library, by __graft_entry__.smoke() to check one small
+ * projection, and by bench.py as the timed CPU baseline.  The product never links or calls
  * it.  All pointers here are HOST pointers; the parameter structs are the
  * ones of include/so3g_gb300.h.
  *
