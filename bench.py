@@ -169,7 +169,7 @@ def host_inputs(c, seed=0):
                                     proj="ZEA", interpol="bilinear")
     else:
         p = synth.car_projectionist(c["shape"], c.get("res_arcmin", 1.) * ARCMIN, el=el,
-                                    az0=180.)
+                                    az0=180., proj=c.get("proj", "CAR"))
     q = synth.native(p, Q)
     return p, q, dets, resp
 
@@ -795,8 +795,8 @@ def main():
            "l2": "inputs larger than L2 (TOD %.1f GB)" % (c["n_det"] * c["n_time"] * 4 / 1e9),
            "precision": PRECISION[args.pointing] + (
                "" if c["kind"] in ("car", "hp") or args.pointing != "mixed" else
-               " (mixed applies to CAR nearest neighbour and HEALPix; this pixelization "
-               "runs certified)"),
+               " (mixed applies to CAR/TAN/ZEA/SIN nearest neighbour and HEALPix; this "
+               "pixelization runs certified)"),
            "pointing": args.pointing,
            "parallelism": "replicas" if world > 1 else "single GPU"}
 

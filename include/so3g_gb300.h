@@ -96,9 +96,9 @@ enum so3g_pointing {
      * differ from it by one float32 ulp.  Other pixelizations use the
      * exact path. */
     SO3G_POINTING_CERTIFIED = 1,
-    /* Mixed precision (CAR with nearest-neighbour flat pixelizors, and
-     * HEALPix; other pixelizations as SO3G_POINTING_CERTIFIED): float32
-     * pointing whose
+    /* Mixed precision (CAR, TAN, ZEA and SIN with nearest-neighbour flat
+     * pixelizors, and HEALPix; other pixelizations as
+     * SO3G_POINTING_CERTIFIED): float32 pointing whose
      * pixel indices are certified equal to the exact ones (samples that
      * cannot be certified take the double-float, then the exact path).
      * Spin factors and from_map terms are float32 evaluations: maps and

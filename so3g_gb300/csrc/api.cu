@@ -150,11 +150,13 @@ __global__ void k_bore_f32(const double *bore, float4 *out, int n_time) {
 const float4 *bore_f32(const so3g_pixelization *pz, int mode, const double *bore, int n_time,
                        cudaStream_t stream) {
     const int kind = pix_kind(pz);
-    if (mode != SO3G_POINTING_MIXED || pz->coord_sys != SO3G_COORD_CAR ||
-        (kind != PX_FLAT_NT_NN && kind != PX_FLAT_T_NN && kind != PX_HP_NT &&
-         kind != PX_HP_T) ||
-        n_time <= 0 || !bore)
-        return nullptr;
+    const int cs = pz->coord_sys;
+    const bool flat_nn = kind == PX_FLAT_NT_NN || kind == PX_FLAT_T_NN;
+    const bool hp = kind == PX_HP_NT || kind == PX_HP_T;
+    const bool eligible = (hp && cs == SO3G_COORD_CAR) ||
+                          (flat_nn && (cs == SO3G_COORD_CAR || cs == SO3G_COORD_TAN ||
+                                       cs == SO3G_COORD_ZEA || cs == SO3G_COORD_SIN));
+    if (mode != SO3G_POINTING_MIXED || !eligible || n_time <= 0 || !bore) return nullptr;
     float4 *p = nullptr;
     if (cudaMallocAsync(reinterpret_cast<void **>(&p), sizeof(float4) * (size_t)n_time,
                         stream) != cudaSuccess) {

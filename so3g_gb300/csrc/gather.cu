@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(kBlock, MODE == 2 ? 7 : 5) k_from_map(GatherAr
                 int pix[3];
                 float pf[3];
                 bool on = false;
-                if (mixed_pointing<P>(a.g, a.ft, a.mc, qb, qd32, nc, T, Pr, pix, on, pf)) {
+                if (mixed_pointing<C, P>(a.g, a.ft, a.mc, qb, qd32, nc, T, Pr, pix, on, pf)) {
                     if (on) {
                         long long off, plane;
                         const int bad = locate<P>(a.g, pix, &off, &plane);

@@ -1,6 +1,6 @@
 // mixedpoint.cuh -- float32 pointing with certified pixel indices
-// (SO3G_POINTING_MIXED), for CAR with a nearest-neighbour flat pixelizor
-// and for HEALPix.
+// (SO3G_POINTING_MIXED), for CAR, TAN, ZEA and SIN with nearest-neighbour
+// flat pixelizors and for HEALPix.
 //
 // The sample's quaternion product, table lookups, pixel coordinates and
 // spin factors are evaluated in plain float32.  Alongside, a bound on the
@@ -37,8 +37,10 @@ struct FastEligible {
 template <int C, int P>
 struct MixedEligible {
     static constexpr bool value =
-        C == SO3G_COORD_CAR &&
-        (P == PX_FLAT_NT_NN || P == PX_FLAT_T_NN || P == PX_HP_NT || P == PX_HP_T);
+        ((C == SO3G_COORD_CAR || C == SO3G_COORD_TAN || C == SO3G_COORD_ZEA ||
+          C == SO3G_COORD_SIN) &&
+         (P == PX_FLAT_NT_NN || P == PX_FLAT_T_NN)) ||
+        (C == SO3G_COORD_CAR && (P == PX_HP_NT || P == PX_HP_T));
 };
 
 
@@ -227,22 +229,20 @@ __device__ __forceinline__ bool floor_cert(float v, float e, int &i) {
     return r > e && r < 1.f - e;
 }
 
-// The float32 tier for CAR with a nearest-neighbour flat pixelizor.
-// Returns false when the sample must go to the double-float path.
+// The flat pixelizor step of the float32 tier: pixel coordinates x = X /
+// cdx + crpix_x - 1 + 0.5 (and y) from projection-plane coordinates (X, Y)
+// with error bounds (eX, eY), the float32 roundings of 1/cdx, of the offset
+// and of the fma added, x1.5 safety; false when an integer part is not
+// certain.
 template <int P>
-__device__ __forceinline__ bool mixed_car(const DGeom &g, const FastTables &ft,
-                                          const MixedConst &mc, const float (&qb)[4],
-                                          const float (&qd)[4], int nc, float T, float Pr,
-                                          int *pix, bool &on, float *pf) {
-    MixedLonLat o;
-    if (!mixed_lonlat(ft, mc, qb, qd, o)) return false;
-    // Pixel coordinates x = lon / cdx + crpix_x - 1 + 0.5 (and y), with the
-    // float32 rounding of 1/cdx, of the offset and of the fma; x1.5 safety.
-    const float lx = o.lon * mc.inv_cdx, ly = o.lat * mc.inv_cdy;
-    const float x = fmaf(o.lon, mc.inv_cdx, mc.off_x), y = fmaf(o.lat, mc.inv_cdy, mc.off_y);
-    const float ex = 1.5f * fmaf(fabsf(mc.inv_cdx), o.elon,
+__device__ __forceinline__ bool mixed_flat_pixel(const DGeom &g, const MixedConst &mc, float X,
+                                                 float Y, float eX, float eY, int *pix,
+                                                 bool &on) {
+    const float lx = X * mc.inv_cdx, ly = Y * mc.inv_cdy;
+    const float x = fmaf(X, mc.inv_cdx, mc.off_x), y = fmaf(Y, mc.inv_cdy, mc.off_y);
+    const float ex = 1.5f * fmaf(fabsf(mc.inv_cdx), eX,
                                  kU * (fabsf(lx) + fabsf(mc.off_x) + fabsf(x)));
-    const float ey = 1.5f * fmaf(fabsf(mc.inv_cdy), o.elat,
+    const float ey = 1.5f * fmaf(fabsf(mc.inv_cdy), eY,
                                  kU * (fabsf(ly) + fabsf(mc.off_y) + fabsf(y)));
     int ix, iy;
     if (!(floor_cert(x, ex, ix) & floor_cert(y, ey, iy))) return false;
@@ -262,7 +262,89 @@ __device__ __forceinline__ bool mixed_car(const DGeom &g, const FastTables &ft,
             pix[2] = tx - sub_x * g.tx;
         }
     }
+    return true;
+}
+
+// The float32 tier for CAR with a nearest-neighbour flat pixelizor.
+// Returns false when the sample must go to the double-float path.
+template <int P>
+__device__ __forceinline__ bool mixed_car(const DGeom &g, const FastTables &ft,
+                                          const MixedConst &mc, const float (&qb)[4],
+                                          const float (&qd)[4], int nc, float T, float Pr,
+                                          int *pix, bool &on, float *pf) {
+    MixedLonLat o;
+    if (!mixed_lonlat(ft, mc, qb, qd, o)) return false;
+    if (!mixed_flat_pixel<P>(g, mc, o.lon, o.lat, o.elon, o.elat, pix, on)) return false;
     if (on) mixed_spin(o, nc, T, Pr, pf);
+    return true;
+}
+
+// The float32 tier for the zenithal projections (Pointer<ProjTAN|ProjZEA|
+// ProjSIN>::GetCoords, :337-437) with a nearest-neighbour flat pixelizor.
+// With n = a^2 + d^2 = cos^2(theta/2), u = ab - cd, v = ac + bd ((u, v)
+// has length sin(theta)/2): SIN (X, Y) = 2 (u, v), TAN 2 (u, v) / (2n - 1),
+// ZEA 2 (u, v) / sqrt(n).  Error bounds: the rotation error 2|dq| <= 20u
+// moves the point on the sphere by <= 20u, which moves (X, Y) by <= 20u
+// (SIN), 20u / cos(theta)^2 (TAN) or 20u / cos(theta/2) (ZEA); |q~|^2 = 1
+// +- 20u scales u, v and n; plus the float32 roundings.  False (double-
+// float path) far from the projection's pole: TAN with cos(theta) < 0.1,
+// ZEA and SIN with n < 0.25 (theta > 120 deg).
+template <int C, int P>
+__device__ __forceinline__ bool mixed_zen(const DGeom &g, const MixedConst &mc,
+                                          const float (&qb)[4], const float (&qd)[4], int nc,
+                                          float T, float Pr, int *pix, bool &on, float *pf) {
+    const float a = fmaf(qb[0], qd[0], fmaf(-qb[1], qd[1], fmaf(-qb[2], qd[2], -qb[3] * qd[3])));
+    const float b = fmaf(qb[0], qd[1], fmaf(qb[1], qd[0], fmaf(qb[2], qd[3], -qb[3] * qd[2])));
+    const float c = fmaf(qb[0], qd[2], fmaf(-qb[1], qd[3], fmaf(qb[2], qd[0], qb[3] * qd[1])));
+    const float d = fmaf(qb[0], qd[3], fmaf(qb[1], qd[2], fmaf(-qb[2], qd[1], qb[3] * qd[0])));
+    const float n = fmaf(a, a, d * d);
+    if (!(n > 0.25f)) return false;
+    const float u = fmaf(a, b, -c * d), v = fmaf(a, c, b * d);
+    float X, Y, e;
+    if (C == SO3G_COORD_SIN) {
+        X = 2.f * u;
+        Y = 2.f * v;
+        e = fmaf(21.f * kU, fabsf(X) + fabsf(Y), 24.f * kU);
+    } else if (C == SO3G_COORD_TAN) {
+        const float ct = fmaf(2.f, n, -1.f);
+        if (!(ct > 0.1f)) return false;
+        const float r = __frcp_rn(ct);
+        X = 2.f * u * r;
+        Y = 2.f * v * r;
+        // 20u sec^2 (rotation) + 2u sec (u's and v's absolute rounding,
+        // <= u) + |P| (24u: their norm scaling and the reciprocal's and
+        // products' roundings; 44u sec: the norm and roundings of 2n - 1).
+        e = fmaf(fmaf(20.f * kU, r, 2.f * kU), r,
+                 (fabsf(X) + fabsf(Y)) * fmaf(44.f * kU, r, 30.f * kU));
+    } else {
+        const float r = rsqrtf(n) * (1.f + 4.f * kU);   // >= 1/sqrt(n)
+        const float sq = sqrtf(n);
+        X = 2.f * u / sq;
+        Y = 2.f * v / sq;
+        // 20u / cos(theta/2) (rotation) + 2u / cos(theta/2) (u's and v's
+        // absolute rounding, <= u) + |P| (10u: norm, 6u: roundings).
+        e = fmaf(22.f * kU, r, 16.f * kU * (fabsf(X) + fabsf(Y)));
+    }
+    if (!mixed_flat_pixel<P>(g, mc, X, Y, e, e, pix, on)) return false;
+    if (!on) return true;
+    // Spin factors (:1180-1209) with c = (a^2 - d^2)/n, s = 2ad/n.
+    if (nc == 1) {
+        pf[0] = T;
+        pf[1] = pf[2] = 0.f;
+        return true;
+    }
+    const float N1 = fmaf(a, a, -d * d), N2 = 2.f * a * d;
+    const float k = Pr * __frcp_rn(n * n);
+    const float v1 = fmaf(N1, N1, -N2 * N2) * k, v2 = 2.f * N1 * N2 * k;
+    if (nc == 2) {
+        pf[0] = v1;
+        pf[1] = v2;
+        pf[2] = 0.f;
+    } else {
+        pf[0] = T;
+        pf[1] = v1;
+        pf[2] = v2;
+    }
     return true;
 }
 
@@ -367,7 +449,7 @@ __device__ __forceinline__ bool mixed_healpix(const DGeom &g, const FastTables &
 
 // The float32 tier of one sample for pixelization P: one tap (weight 1)
 // when `on`.  False hands the sample to the double-float path.
-template <int P>
+template <int C, int P>
 __device__ __forceinline__ bool mixed_pointing(const DGeom &g, const FastTables &ft,
                                                const MixedConst &mc, const float (&qb)[4],
                                                const float (&qd)[4], int nc, float T, float Pr,
@@ -376,7 +458,8 @@ __device__ __forceinline__ bool mixed_pointing(const DGeom &g, const FastTables 
         on = true;
         return mixed_healpix<P>(g, ft, mc, qb, qd, nc, T, Pr, pix, pf);
     }
-    return mixed_car<P>(g, ft, mc, qb, qd, nc, T, Pr, pix, on, pf);
+    if (C == SO3G_COORD_CAR) return mixed_car<P>(g, ft, mc, qb, qd, nc, T, Pr, pix, on, pf);
+    return mixed_zen<C, P>(g, mc, qb, qd, nc, T, Pr, pix, on, pf);
 }
 
 }  // namespace so3g

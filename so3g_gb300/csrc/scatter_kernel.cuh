@@ -253,7 +253,7 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
                 float qb[4];
                 load_bore_f32(a.bore32, a.bore, t, qb);
                 bool on = false;
-                if (mixed_pointing<P>(a.g, a.ft, a.mc, qb, qd32, nc, T, Pr, pix[0], on, pf)) {
+                if (mixed_pointing<C, P>(a.g, a.ft, a.mc, qb, qd32, nc, T, Pr, pix[0], on, pf)) {
                     n = on ? 1 : 0;
                     w[0] = 1.f;
                 } else {

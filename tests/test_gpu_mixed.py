@@ -1,5 +1,5 @@
-"""Mixed-precision pointing (POINTING_MIXED, CAR nearest neighbour): pixel
-indices bit-identical to the exact float64 path, sample by sample and on
+"""Mixed-precision pointing (POINTING_MIXED: CAR, TAN, ZEA and SIN nearest
+neighbour, and HEALPix): pixel indices bit-identical to the exact float64 path, sample by sample and on
 pixel edges; spin factors, maps and signals within the mixed-precision
 tolerance (1e-6 of their scale) of the exact path."""
 import numpy as np
@@ -167,3 +167,53 @@ def test_mixed_healpix_edges():
     for nest in (False, True):
         p, eng = _hp_engine(nside, nest, False)
         _probe_hp(eng, q, dets, resp, False)
+
+
+@pytest.mark.parametrize("proj", ["TAN", "ZEA", "SIN"])
+@pytest.mark.parametrize("tiled", [False, True])
+def test_mixed_zenithal_at_scale(proj, tiled):
+    Q, dets, resp, gamma, _ = synth.workload(100, 100_000, seed=65, radius_deg=1.0)
+    p, eng = _engine((900, 1100), 0.25 * ARCMIN, tiled, proj=proj)
+    q = synth.native(p, Q)
+    res = _probe(eng, q, dets, resp, tiled)
+    assert 0.2 < (res[0] > 0).mean() < 1.0
+
+
+@pytest.mark.parametrize("proj", ["TAN", "ZEA", "SIN"])
+def test_mixed_zenithal_edges(orc, proj):
+    """Zenithal samples on pixel edges (and 1e-13 .. 1e-5 either side)."""
+    from test_gpu_certified import _solve_lonlat
+    rng = np.random.default_rng(67)
+    p, eng = _engine((300, 400), 0.5 * ARCMIN, False, proj=proj)
+    (ny, nx) = eng.naxis
+    n = 20000
+    ix = rng.integers(-2, nx + 2, n).astype(float)
+    iy = rng.integers(-2, ny + 2, n).astype(float)
+    jit = rng.choice([0., 1e-13, -1e-13, 1e-9, -1e-6, 1e-5, 0.5], n)
+    gam = rng.uniform(0, np.pi, n)
+    (dy, dx), (cry, crx) = eng.cdelt, eng.crpix
+    u = (ix + jit - (crx - 0.5)) * abs(dx)
+    v = (iy + jit - (cry - 0.5)) * dy
+    lon, lat = _solve_lonlat(orc, eng, ix + jit, iy + jit, np.arctan2(u, v),
+                             np.pi / 2 - np.hypot(u, v), gam)
+    q = _quats_at(lon, lat, gam)
+    dets = np.array([[1., 0., 0., 0.], [np.cos(0.3), 0., 0., np.sin(0.3)]])
+    resp = np.array([[1., 1.], [0.7, 0.45]], np.float32)
+    _probe(eng, q, dets, resp, False)
+
+
+@pytest.mark.parametrize("proj", ["TAN", "ZEA", "SIN"])
+def test_mixed_zenithal_whole_sky(proj):
+    """Samples over the whole sphere on a wide zenithal map: the float32
+    tier's guard sends the far side (and TAN's horizon) to the exact tiers
+    and every pixel index stays equal."""
+    rng = np.random.default_rng(69)
+    p, eng = _engine((240, 240), 30 * ARCMIN, False, proj=proj)
+    n = 40000
+    lon = rng.uniform(-np.pi, np.pi, n)
+    lat = np.arcsin(rng.uniform(-1, 1, n))
+    q = _quats_at(lon, lat, rng.uniform(0, np.pi, n))
+    dets = np.array([[1., 0., 0., 0.], [np.cos(0.3), 0., 0., np.sin(0.3)]])
+    resp = np.array([[1., 1.], [0.7, 0.45]], np.float32)
+    res = _probe(eng, q, dets, resp, False)
+    assert (res[0] > 0).mean() > 0.05
