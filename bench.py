@@ -473,8 +473,12 @@ def run_e2e(args, c, eng, q, dets, resp, sig_dev, dev):
     nb_point = q_h.numel() * 8 + d_h.numel() * 8 + r_h.numel() * 4
     h2d = nb_sig + nb_map + nb_point + nb_sig + nb_map + nb_point
     d2h = nb_map + nb_sig
+    from so3g_gb300 import projeng
     return {"value": N / dt, "unit": "samples/s", "h2d_bytes_per_step": int(h2d),
-            "d2h_bytes_per_step": int(d2h), "ms_per_step": dt * 1e3}
+            "d2h_bytes_per_step": int(d2h), "ms_per_step": dt * 1e3,
+            "host_signal": "page-locked, policy %s (%s)" % (
+                projeng.host_signal_policy(),
+                "used in place" if projeng._host_direct(sig_h, True) else "streamed")}
 
 
 # ---------------------------------------------------------------------------

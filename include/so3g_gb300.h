@@ -12,7 +12,9 @@
  *   - Array arguments of the so3g_proj_* and so3g_precomp_* entry points
  *     are DEVICE pointers (memory of the current CUDA device), except the
  *     structs themselves, which live in host memory and are read before the
- *     call returns.
+ *     call returns.  The signal of so3g_proj_to_map / so3g_proj_from_map
+ *     may also be host memory that the device reaches in place (see
+ *     so3g_host_access).
  *   - Work is enqueued on `stream` (a cudaStream_t; NULL = legacy default
  *     stream).  Calls return once the kernels are enqueued; results are
  *     ordered on the stream.
@@ -191,6 +193,27 @@ int so3g_get_trig_tables(double *asin_vals, double *atan2_vals, int32_t n);
 
 /* Number of kernel launches this library has enqueued since load. */
 int64_t so3g_launch_count(void);
+
+/* How the current device can reach host memory at `ptr` (no counterpart
+ * in the reference, whose arrays are all host memory).  Sets *mode to
+ *   SO3G_HOST_NONE     not reachable: copy it to the device first;
+ *   SO3G_HOST_MAPPED   page-locked memory mapped into the device's address
+ *                      space at the same address (cudaHostAlloc /
+ *                      cudaHostRegister under unified addressing);
+ *   SO3G_HOST_PAGEABLE ordinary (pageable) memory, which this device reads
+ *                      and writes coherently through the host's page
+ *                      tables (cudaDevAttrPageableMemoryAccess, e.g. a
+ *                      Grace host over NVLink-C2C).
+ * The signal pointer of so3g_proj_to_map / so3g_proj_from_map may be such
+ * host memory when the mode is not SO3G_HOST_NONE: the kernels then read
+ * (and from_map writes) the samples in place, with no staging copy.  A
+ * NULL ptr gives SO3G_HOST_NONE. */
+enum so3g_host_mode {
+    SO3G_HOST_NONE     = 0,
+    SO3G_HOST_MAPPED   = 1,
+    SO3G_HOST_PAGEABLE = 2
+};
+int so3g_host_access(const void *ptr, int32_t *mode);
 
 /* ---- Pointing-only queries ----------------------------------------------- */
 

@@ -20,6 +20,7 @@ ACCUM_ATOMIC, ACCUM_WARP_RUNS = 0, 1
 DEVERR_NONE, DEVERR_MISSING_TILE, DEVERR_PIXEL_RANGE = 0, 1, 2
 ABI_VERSION = 2
 POINTING_EXACT, POINTING_CERTIFIED, POINTING_MIXED = 0, 1, 2
+HOST_NONE, HOST_MAPPED, HOST_PAGEABLE = 0, 1, 2
 LUT_N = 1 << 14
 
 c_int32 = ctypes.c_int32
@@ -92,6 +93,7 @@ _SIGS = {
     "so3g_abi_version": (ctypes.c_int, []),
     "so3g_get_trig_tables": (ctypes.c_int, [c_void_p, c_void_p, c_int32]),
     "so3g_launch_count": (c_int64, []),
+    "so3g_host_access": (ctypes.c_int, [c_void_p, c_void_p]),
     "so3g_proj_coords": (ctypes.c_int, [P(Pixelization), c_void_p, c_int32, c_void_p, c_int32,
                                         c_void_p, c_void_p]),
     "so3g_proj_pixels": (ctypes.c_int, [P(Pixelization), c_void_p, c_int32, c_void_p, c_int32,

@@ -323,6 +323,37 @@ int so3g_init(void) {
     return SO3G_OK;
 }
 
+int so3g_host_access(const void *ptr, int32_t *mode) {
+    clear_error();
+    if (!mode) return set_error(SO3G_ERR_ARGUMENT, "mode is NULL");
+    *mode = SO3G_HOST_NONE;
+    if (!ptr) return SO3G_OK;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_error(SO3G_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+    cudaPointerAttributes at{};
+    e = cudaPointerGetAttributes(&at, ptr);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(SO3G_ERR_CUDA, "cudaPointerGetAttributes: %s", cudaGetErrorString(e));
+    }
+    if (at.type == cudaMemoryTypeHost) {
+        // Page-locked: usable in kernels when mapped at the same address.
+        if (at.devicePointer == ptr) *mode = SO3G_HOST_MAPPED;
+        return SO3G_OK;
+    }
+    if (at.type == cudaMemoryTypeUnregistered) {
+        int pageable = 0;
+        e = cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(SO3G_ERR_CUDA, "cudaDeviceGetAttribute: %s", cudaGetErrorString(e));
+        }
+        if (pageable == 1) *mode = SO3G_HOST_PAGEABLE;
+    }
+    return SO3G_OK;
+}
+
 int so3g_get_trig_tables(double *asin_vals, double *atan2_vals, int32_t n) {
     clear_error();
     if (n != kLutN) return set_error(SO3G_ERR_ARGUMENT, "table size is %d", kLutN);

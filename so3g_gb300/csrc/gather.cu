@@ -172,6 +172,11 @@ __global__ void __launch_bounds__(kBlock, MODE == 2 ? 7 : 5) k_from_map(GatherAr
         bool push = false, push_df = false;
         if (kMixedOK && mixed) {
             if (t < t1) {
+                // The signal is loaded before the pointing is evaluated, so
+                // that the load's latency (long for a signal in host memory)
+                // overlaps the pointing arithmetic.
+                float *sp = a.signal + det * a.sig_stride + t;
+                const float s_in = *sp;
                 float qb[4];
                 load_bore_f32(a.bore32, a.bore, t, qb);
                 int pix[3];
@@ -185,8 +190,7 @@ __global__ void __launch_bounds__(kBlock, MODE == 2 ? 7 : 5) k_from_map(GatherAr
                             record_missing_tile(a.err, bad);
                         } else {
                             // float32 terms (the mixed-precision contract).
-                            float *sp = a.signal + det * a.sig_stride + t;
-                            float s = *sp;
+                            float s = s_in;
                             if (a.map32) {
                                 const float4 m = __ldg(a.map32 + off);
                                 s = fmaf(m.x, pf[0], s);
@@ -223,6 +227,8 @@ __global__ void __launch_bounds__(kBlock, MODE == 2 ? 7 : 5) k_from_map(GatherAr
             continue;
         }
         if (t < t1) {
+            float *sp = a.signal + det * a.sig_stride + t;
+            const float s_in = *sp;   // loaded early, as in the mixed branch
             const double *bp = a.bore + 4LL * t;
             const double2 lo = __ldg(reinterpret_cast<const double2 *>(bp));
             const double2 hi = __ldg(reinterpret_cast<const double2 *>(bp) + 1);
@@ -236,8 +242,7 @@ __global__ void __launch_bounds__(kBlock, MODE == 2 ? 7 : 5) k_from_map(GatherAr
             if (ok && n > 0) {
                 // src/Projection.cxx:1763-1765 with certified float32
                 // roundings, tap by tap and component by component.
-                float *sp = a.signal + det * a.sig_stride + t;
-                float s = *sp;
+                float s = s_in;
 #pragma unroll
                 for (int k = 0; k < NT; k++) {
                     if (k >= n || !ok) break;

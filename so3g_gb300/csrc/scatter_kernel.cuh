@@ -247,6 +247,10 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
         int n = 0;
         float sig = 0.f;
         bool push = false, push_df = false;
+        // The sample's signal is loaded before its pointing is evaluated, so
+        // that the load's latency (long for a signal in host memory, read
+        // over the host link) overlaps the pointing arithmetic.
+        const float sig_in = (!WEIGHT && live) ? __ldg(a.signal + det * a.sig_stride + t) : 0.f;
         if (live) {
             bool done = false;
             if (kMixedOK && mixed) {
@@ -281,7 +285,7 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
                 spin_factors(nc, coords, T, Pr, pf);
                 n = get_pixels<P>(a.g, coords, pix, w);
             }
-            if (!WEIGHT && n > 0) sig = __ldg(a.signal + det * a.sig_stride + t);
+            if (!WEIGHT && n > 0) sig = sig_in;
         }
         // (Mixed pointing fills the exact queue from the double-float pass.)
         if (kFastOK && fast && !mixed) qn = warp_enqueue(wq, qn, push, t);

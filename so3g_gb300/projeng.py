@@ -12,10 +12,14 @@ argument order and meaning, return values, in-place mutation of ``map`` and
 Arguments may be numpy arrays (or other buffer-protocol objects), CPU torch
 tensors or CUDA torch tensors.  Host arguments are copied to the current
 CUDA device, the kernels run, and outputs are copied back into the caller's
-arrays before the call returns.  CUDA tensors are used in place on the
+arrays before the call returns; a large host signal that the device can
+reach in place (page-locked, or pageable on a host with coherent device
+access) is instead read and written by the kernels where it lies, and one
+that it cannot is streamed through the device in chunks.  CUDA tensors are used in place on the
 current stream (no copies); outputs created by the call are then CUDA
 tensors too.  Every call runs the CUDA kernels: there is no CPU path.
 """
+import ctypes
 import os
 
 import numpy as np
@@ -421,6 +425,69 @@ def _host_matrix(sig):
             return None
         t = torch.from_numpy(a)
     return t if t.numel() * 4 >= STREAM_MIN_BYTES else None
+
+
+# A host signal that the device can reach in place -- page-locked memory
+# mapped into the device's address space, or ordinary memory on a host whose
+# GPUs access pageable memory coherently (a Grace host over NVLink-C2C) --
+# can be read and written by the kernels directly: the samples then cross
+# the link once, inside the kernel, with no staging buffers.  Measured on a
+# GB300 (1000 det x 1M samples, CAR TQU): the copy engines move page-locked
+# memory faster than the kernels read it in place (to_map 20.9 ms streamed,
+# 25.5 ms in place; from_map 30.1 against 40.7 ms), while a pageable signal
+# is read faster in place (to_map 25.8 against 29.3-31.6 ms) but not
+# written (from_map 57 against 53-55 ms).  SO3G_GB300_HOST_SIGNAL selects:
+#   "auto"   (default) in place where that measured faster: a pageable
+#            signal that is only read (to_map);
+#   "direct" in place whenever the device can reach the memory;
+#   "mapped" in place for page-locked memory only;
+#   "stream" never in place.
+_HOST_POLICIES = ("auto", "direct", "mapped", "stream")
+
+
+def host_signal_policy():
+    """The host-signal policy named by SO3G_GB300_HOST_SIGNAL."""
+    name = os.environ.get("SO3G_GB300_HOST_SIGNAL", "auto")
+    if name not in _HOST_POLICIES:
+        raise ValueError("SO3G_GB300_HOST_SIGNAL must be one of %s (got %r)"
+                         % (", ".join(_HOST_POLICIES), name))
+    return name
+
+
+def _host_mode(host):
+    """so3g_host_access mode of the memory of the CPU tensor `host`."""
+    _device()
+    mode = ctypes.c_int32(0)
+    _abi.check(_abi.lib().so3g_host_access(host.data_ptr(), ctypes.byref(mode)),
+               "host_access")
+    return mode.value
+
+
+def _host_direct(host, writes):
+    """True if the kernels should use the CPU tensor `host` in place under
+    host_signal_policy(); `writes`: the call writes the signal."""
+    policy = host_signal_policy()
+    if policy == "stream":
+        return False
+    mode = _host_mode(host)
+    if policy == "direct":
+        return mode != _abi.HOST_NONE
+    if policy == "mapped":
+        return mode == _abi.HOST_MAPPED
+    return mode == _abi.HOST_PAGEABLE and not writes
+
+
+def _run_host(host, launch, upload, download):
+    """launch() over the host signal matrix `host`: in place when
+    _host_direct() says so, else streamed through device buffers
+    (_stream_rows).  Returns when the results are in host memory."""
+    if host.shape[0] == 0 or host.shape[1] == 0:
+        return
+    if _host_direct(host, download):
+        launch(0, host.shape[0], host)
+        torch.cuda.current_stream().synchronize()
+        return
+    _stream_rows(host, launch, upload, download)
 
 
 def _stream_rows(host, launch, upload, download):
@@ -876,7 +943,7 @@ class ProjEngBase:
 
         host = _host_matrix(sig)
         if host is not None:
-            _stream_rows(host, launch, upload=True, download=True)
+            _run_host(host, launch, upload=True, download=True)
             err.raise_if_set()
             return sig.ret
         sig.upload()
@@ -911,7 +978,7 @@ class ProjEngBase:
                     None if w is None else w.data_ptr() + 4 * d0, None, m.struct, acc,
                     err.ptr, _stream()), "to_map")
 
-            _stream_rows(host, launch, upload=True, download=False)
+            _run_host(host, launch, upload=True, download=False)
         else:
             sig.upload()
             rng.upload()

@@ -1,7 +1,10 @@
-"""Host signals streamed through the device in chunks of detector rows
-(to_map and from_map with numpy arrays or CPU tensors): the results equal
-those of the same call with device tensors, for pageable and pinned host
-memory, with chunk sizes that do and do not divide the detector count."""
+"""Host signals (to_map and from_map with numpy arrays or CPU tensors),
+streamed through the device in chunks of detector rows or read and written
+by the kernels in place: the results equal those of the same call with
+device tensors, for pageable and pinned host memory, with chunk sizes that
+do and do not divide the detector count."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -28,9 +31,20 @@ def _setup(n_det=40, n_time=20000, weights=True):
     return p.get_ProjEng("TQU"), q, dets, resp, sig, w
 
 
+@pytest.mark.parametrize("policy", ["stream", "direct", "mapped", "auto"])
 @pytest.mark.parametrize("host_kind", ["numpy", "torch", "pinned"])
-def test_streamed_to_map_and_from_map(small_chunks, host_kind):
+def test_streamed_to_map_and_from_map(small_chunks, monkeypatch, host_kind, policy):
     import torch
+    from so3g_gb300 import _abi
+    monkeypatch.setenv("SO3G_GB300_HOST_SIGNAL", policy)
+    streamed = []
+    orig = projeng._stream_rows
+
+    def spy(*a, **k):
+        streamed.append(k.get("download", a[3] if len(a) > 3 else None))
+        return orig(*a, **k)
+
+    monkeypatch.setattr(projeng, "_stream_rows", spy)
     eng, q, dets, resp, sig, w = _setup()
     dq, dd, dr, ds, dw = (torch.from_numpy(x).cuda() for x in (q, dets, resp, sig, w))
     want_m = eng.to_map(None, dq, dd, dr, ds, dw, None).cpu().numpy()
@@ -45,7 +59,9 @@ def test_streamed_to_map_and_from_map(small_chunks, host_kind):
         return t.pin_memory() if host_kind == "pinned" else t
 
     m = np.zeros_like(want_m)
-    eng.to_map(m, q, dets, resp, host(sig), w, None)
+    h = host(sig)
+    mode = projeng._host_mode(h if isinstance(h, torch.Tensor) else torch.from_numpy(h))
+    eng.to_map(m, q, dets, resp, h, w, None)
     assert np.abs(m - want_m).max() <= 1e-12 * np.abs(want_m).max()
     s = host(sig0)
     ret = eng.from_map(want_m, q, dets, resp, s)
@@ -55,11 +71,45 @@ def test_streamed_to_map_and_from_map(small_chunks, host_kind):
         assert all(np.shares_memory(r, s) for r in ret)
     else:
         assert ret is s
+    # Which calls streamed (False: to_map, True: from_map).  Page-locked
+    # memory is mapped under unified addressing; pageable memory is
+    # reachable only where the device accesses it coherently.
+    assert mode in ((_abi.HOST_MAPPED,) if host_kind == "pinned"
+                    else (_abi.HOST_NONE, _abi.HOST_PAGEABLE))
+    direct = {
+        "stream": lambda writes: False,
+        "direct": lambda writes: mode != _abi.HOST_NONE,
+        "mapped": lambda writes: mode == _abi.HOST_MAPPED,
+        "auto": lambda writes: mode == _abi.HOST_PAGEABLE and not writes,
+    }[policy]
+    assert streamed == [w for w in (False, True) if not direct(w)]
+
+
+def test_host_access_modes():
+    import torch
+    from so3g_gb300 import _abi
+    projeng._ensure_init()
+    lib = _abi.lib()
+
+    def mode(ptr):
+        m = ctypes.c_int32(-1)
+        assert lib.so3g_host_access(ptr, ctypes.byref(m)) == 0
+        return m.value
+
+    dev = torch.zeros(16, device="cuda")
+    pinned = torch.zeros(16).pin_memory()
+    pageable = np.zeros(1 << 20, np.float32)
+    assert mode(None) == _abi.HOST_NONE
+    assert mode(dev.data_ptr()) == _abi.HOST_NONE
+    assert mode(pinned.data_ptr()) == _abi.HOST_MAPPED
+    assert mode(pageable.ctypes.data) in (_abi.HOST_NONE, _abi.HOST_PAGEABLE)
+    assert lib.so3g_host_access(None, None) == -1
 
 
 def test_stream_threshold(monkeypatch):
     """Signals below the threshold, lists of rows and thread_intervals go
     through the device whole."""
+    monkeypatch.setenv("SO3G_GB300_HOST_SIGNAL", "stream")
     eng, q, dets, resp, sig, w = _setup(n_det=8, n_time=5000)
     calls = []
     orig = projeng._stream_rows

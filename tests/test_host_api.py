@@ -222,3 +222,15 @@ def test_install_as_so3g():
     import so3g
     assert so3g.ProjEng_CAR_TQU_NonTiled is so3g_gb300.ProjEng_CAR_TQU_NonTiled
     assert so3g.useful_info()["omp_num_threads"] >= 1
+
+
+def test_host_signal_policy(monkeypatch):
+    from so3g_gb300 import projeng
+    monkeypatch.delenv("SO3G_GB300_HOST_SIGNAL", raising=False)
+    assert projeng.host_signal_policy() == "auto"
+    for name in ("auto", "direct", "mapped", "stream"):
+        monkeypatch.setenv("SO3G_GB300_HOST_SIGNAL", name)
+        assert projeng.host_signal_policy() == name
+    monkeypatch.setenv("SO3G_GB300_HOST_SIGNAL", "bogus")
+    with pytest.raises(ValueError, match="SO3G_GB300_HOST_SIGNAL"):
+        projeng.host_signal_policy()
