@@ -445,23 +445,33 @@ def run_e2e(args, c, eng, q, dets, resp, sig_dev, dev):
     import torch
     sig_h = torch.empty(sig_dev.shape, dtype=torch.float32, pin_memory=True)
     sig_h.copy_(sig_dev)
-    out_h = torch.zeros(sig_dev.shape, dtype=torch.float32, pin_memory=True)
     q_h = torch.from_numpy(q).pin_memory()
     d_h = torch.from_numpy(dets).pin_memory()
     r_h = torch.from_numpy(resp).pin_memory()
     ny, nx = c["shape"]
     m_h = torch.zeros((3, ny, nx), dtype=torch.float64).pin_memory()
 
+    parts = {"to_map": [], "from_map": []}
+
     def step():
+        # to_map of the host signal into the host map, then from_map of that
+        # map into a new host signal (signal=None, as a map-maker's P m).
         m_h.zero_()
+        t0 = time.perf_counter()
         eng.to_map(m_h, q_h, d_h, r_h, sig_h, None, None)
-        out_h.zero_()
-        eng.from_map(m_h, q_h, d_h, r_h, out_h)
+        t1 = time.perf_counter()
+        out = eng.from_map(m_h, q_h, d_h, r_h, None)
+        t2 = time.perf_counter()
+        assert len(out) == sig_h.shape[0]
+        parts["to_map"].append((t1 - t0) * 1e3)
+        parts["from_map"].append((t2 - t1) * 1e3)
 
     for _ in range(max(1, args.warmup)):
         step()
     torch.cuda.synchronize()
     steps = max(1, args.steps // 2)
+    for v in parts.values():
+        v.clear()
     t0 = time.perf_counter()
     for _ in range(steps):
         step()
@@ -471,14 +481,19 @@ def run_e2e(args, c, eng, q, dets, resp, sig_dev, dev):
     nb_sig = sig_h.numel() * 4
     nb_map = m_h.numel() * 8
     nb_point = q_h.numel() * 8 + d_h.numel() * 8 + r_h.numel() * 4
-    h2d = nb_sig + nb_map + nb_point + nb_sig + nb_map + nb_point
+    # to_map: signal, map and pointing in, map out; from_map: map and
+    # pointing in, the new signal out.
+    h2d = nb_sig + nb_map + nb_point + nb_map + nb_point
     d2h = nb_map + nb_sig
     from so3g_gb300 import projeng
     return {"value": N / dt, "unit": "samples/s", "h2d_bytes_per_step": int(h2d),
             "d2h_bytes_per_step": int(d2h), "ms_per_step": dt * 1e3,
-            "host_signal": "page-locked, policy %s (%s)" % (
+            "op_ms": {k: float(np.median(v)) for k, v in parts.items()},
+            "step": "to_map(host map, page-locked host signal) + from_map(host map, "
+                    "signal=None) -> new host signal",
+            "host_signal": "policy %s: to_map input %s" % (
                 projeng.host_signal_policy(),
-                "used in place" if projeng._host_direct(sig_h, True) else "streamed")}
+                "used in place" if projeng._host_direct(sig_h, False) else "streamed")}
 
 
 # ---------------------------------------------------------------------------

@@ -480,10 +480,13 @@ def _host_direct(host, writes):
 def _run_host(host, launch, upload, download):
     """launch() over the host signal matrix `host`: in place when
     _host_direct() says so, else streamed through device buffers
-    (_stream_rows).  Returns when the results are in host memory."""
+    (_stream_rows).  upload=False: the kernels start from zeros instead of
+    the contents of `host`.  Returns when the results are in host memory."""
     if host.shape[0] == 0 or host.shape[1] == 0:
         return
     if _host_direct(host, download):
+        if not upload:
+            host.zero_()
         launch(0, host.shape[0], host)
         torch.cuda.current_stream().synchronize()
         return
@@ -946,6 +949,14 @@ class ProjEngBase:
             _run_host(host, launch, upload=True, download=True)
             err.raise_if_set()
             return sig.ret
+        if sig._create and not sig.device_mode and 4 * n_det * n_time >= STREAM_MIN_BYTES:
+            # A new host signal (signal=None): page-locked (torch caches
+            # such blocks across calls), filled by zeroed device chunks and
+            # copied out; nothing is copied in.
+            out = torch.empty((n_det, n_time), dtype=torch.float32, pin_memory=True)
+            _run_host(out, launch, upload=False, download=True)
+            err.raise_if_set()
+            return list(out.numpy())
         sig.upload()
         launch(0, n_det, sig.dev)
         err.raise_if_set()

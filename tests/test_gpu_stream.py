@@ -127,3 +127,20 @@ def test_stream_threshold(monkeypatch):
     m2 = eng.to_map(None, q, dets, resp, list(sig), None, None)
     assert len(calls) == 1
     assert np.abs(m1 - m2).max() <= 1e-12 * np.abs(m1).max()
+
+
+@pytest.mark.parametrize("policy", ["stream", "direct"])
+def test_from_map_new_host_signal(small_chunks, monkeypatch, policy):
+    """from_map with signal=None and host pointing: a new host signal,
+    filled chunk by chunk (or in place), equal to the device result."""
+    import torch
+    monkeypatch.setenv("SO3G_GB300_HOST_SIGNAL", policy)
+    eng, q, dets, resp, sig, w = _setup()
+    dq, dd, dr = (torch.from_numpy(x).cuda() for x in (q, dets, resp))
+    m = eng.to_map(None, q, dets, resp, sig, None, None)
+    want = eng.from_map(torch.from_numpy(m).cuda(), dq, dd, dr, None).cpu().numpy()
+    for _ in range(2):
+        got = eng.from_map(m, q, dets, resp, None)
+        assert isinstance(got, list) and len(got) == len(dets)
+        assert all(isinstance(r, np.ndarray) and r.shape == (q.shape[0],) for r in got)
+        assert np.array_equal(np.stack(got).view(np.int32), want.view(np.int32))
