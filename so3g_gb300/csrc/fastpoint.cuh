@@ -406,6 +406,10 @@ __device__ __forceinline__ bool fast_pixels(const DGeom &g, dfl x, dfl y, int (*
 // Certified spin factors (spin_proj_factors, :1180-1209): float(P * (c*c -
 // s*s)) and float(P * 2*c*s) with c*c - s*s = (Nc^2 - Ns^2)/D and 2*c*s =
 // 2 Nc Ns / D.  Returns false when a float32 rounding is not certain.
+// CERT = false (the mixed-precision contract, where only pixel indices must
+// be the reference's): the floats nearest the double-float values, always
+// accepted.
+template <bool CERT = true>
 __device__ __forceinline__ bool fast_spin(int nc, float T, float Pr, const dfl &Nc,
                                           const dfl &Ns, const dfl &D, float *pf) {
     if (nc == 1) {
@@ -420,9 +424,11 @@ __device__ __forceinline__ bool fast_spin(int nc, float T, float Pr, const dfl &
     // reference rounds to the same float unless its value lies beyond the
     // midpoint to a neighbour, i.e. unless |v.lo| + eps reaches half the
     // gap to the nearer neighbour.
-    const float e = kEpsPf * fmaxf(1.f, 0.25f / D.hi) * fmaxf(1.f, fabsf(Pr));
-    if (!(fabsf(v1.hi) > 1e-30f && fabsf(v1.lo) + e < half_gap(v1.hi))) return false;
-    if (!(fabsf(v2.hi) > 1e-30f && fabsf(v2.lo) + e < half_gap(v2.hi))) return false;
+    if (CERT) {
+        const float e = kEpsPf * fmaxf(1.f, 0.25f / D.hi) * fmaxf(1.f, fabsf(Pr));
+        if (!(fabsf(v1.hi) > 1e-30f && fabsf(v1.lo) + e < half_gap(v1.hi))) return false;
+        if (!(fabsf(v2.hi) > 1e-30f && fabsf(v2.lo) + e < half_gap(v2.hi))) return false;
+    }
     if (nc == 2) {
         pf[0] = v1.hi;
         pf[1] = v2.hi;
@@ -549,8 +555,9 @@ __device__ __forceinline__ bool fast_healpix(const DGeom &g, const FastTables &f
 
 // The certified pointing of one sample: taps (pixels, weights) and spin
 // factors equal to the exact path's (bilinear weights: see fast_pixels).
-// Returns false when the sample must go to the exact path.
-template <int C, int P>
+// Returns false when the sample must go to the exact path.  SPIN_CERT =
+// false: pixels certified, spin factors the nearest floats (fast_spin).
+template <int C, int P, bool SPIN_CERT = true>
 __device__ __forceinline__ bool fast_pointing(const DGeom &g, const FastTables &ft,
                                               const FastConst &fc, const dfl (&qb)[4],
                                               const dfl (&qd)[4], int nc, float T, float Pr,
@@ -564,7 +571,7 @@ __device__ __forceinline__ bool fast_pointing(const DGeom &g, const FastTables &
         if (!fast_lon_spin(ft, fc, a, b, c, d, cos_t, lon, Nc, Ns, D)) return false;
         if (!fast_healpix<P>(g, ft, fc, cos_t, lon, pix, n)) return false;
         w[0] = 1.f;
-        return fast_spin(nc, T, Pr, Nc, Ns, D, pf);
+        return fast_spin<SPIN_CERT>(nc, T, Pr, Nc, Ns, D, pf);
     }
     dfl X, Y, Nc, Ns, D;
     if (!fast_native<C>(ft, fc, qb, qd, X, Y, Nc, Ns, D)) return false;
@@ -572,7 +579,7 @@ __device__ __forceinline__ bool fast_pointing(const DGeom &g, const FastTables &
     const dfl y = df_add(df_mul(Y, fc.inv_cdy), fc.off_y);
     if (!fast_pixels<P>(g, x, y, pix, w, n)) return false;
     if (n == 0) return true;   // off the map: nothing to add
-    return fast_spin(nc, T, Pr, Nc, Ns, D, pf);
+    return fast_spin<SPIN_CERT>(nc, T, Pr, Nc, Ns, D, pf);
 }
 
 // sig + m * pf rounded to float32 as the reference's `*sig += map * pf`

@@ -81,9 +81,10 @@ __device__ __noinline__ void exact_gather(const GatherArgs &a, int det, int t, c
     gather_taps<P, NT>(a, a.signal + det * a.sig_stride + t, n, pix, w, pf);
 }
 
-// One sample through the certified double-float pointing and certified
-// float32 roundings of each term; false (signal untouched) when anything is
-// not certain.
+// One sample of the mixed-pointing fallback through the double-float
+// pointing; false (signal untouched) when its pixel is not certified.  Its
+// spin factors and terms, like the float32 tier's, are float32 evaluations
+// (the mixed-precision contract).
 template <int C, int P>
 __device__ __forceinline__ bool df_gather(const GatherArgs &a, int det, int t, const dfl (&qd)[4], float T,
                           float Pr) {
@@ -99,26 +100,33 @@ __device__ __forceinline__ bool df_gather(const GatherArgs &a, int det, int t, c
     float pf[3], w[NT];
     int n = 0;
     const int nc = a.g.ncomp;
-    if (!fast_pointing<C, P>(a.g, a.ft, a.fc, qb, qd, nc, T, Pr, pix, w, n, pf)) return false;
+    if (!fast_pointing<C, P, false>(a.g, a.ft, a.fc, qb, qd, nc, T, Pr, pix, w, n, pf))
+        return false;
     if (n == 0) return true;
     float *sp = a.signal + det * a.sig_stride + t;
     float s = *sp;
-    bool ok = true;
 #pragma unroll
     for (int k = 0; k < NT; k++) {
-        if (k >= n || !ok) break;
+        if (k >= n) break;
         long long off, plane;
         const int bad = locate<P>(a.g, pix[k], &off, &plane);
         if (bad >= 0) {
             record_missing_tile(a.err, bad);
             continue;
         }
+        if (a.map32) {
+            const float4 m = __ldg(a.map32 + off);
+            s = fmaf(m.x, pf[0] * w[k], s);
+            if (nc > 1) s = fmaf(m.y, pf[1] * w[k], s);
+            if (nc > 2) s = fmaf(m.z, pf[2] * w[k], s);
+        } else {
 #pragma unroll
-        for (int c = 0; c < 3; c++)
-            if (ok && c < nc) ok = fast_accum(s, __ldg(a.map + off + c * plane), pf[c], w[k]);
+            for (int c = 0; c < 3; c++)
+                if (c < nc) s = fmaf(d2f_round(__ldg(a.map + off + c * plane)), pf[c] * w[k], s);
+        }
     }
-    if (ok) *sp = s;
-    return ok;
+    *sp = s;
+    return true;
 }
 
 // Compiled for 5 resident blocks per SM (at most 51 registers; mixed

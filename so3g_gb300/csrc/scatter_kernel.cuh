@@ -129,8 +129,10 @@ __device__ __noinline__ void exact_sample(const ScatterArgs &a, int det, int t, 
     }
 }
 
-// One sample through the certified double-float pointing, added with plain
-// atomics; false (nothing added) when it is not certified.
+// One sample of the mixed-pointing fallback through the double-float
+// pointing, added with plain atomics; false (nothing added) when its pixel
+// is not certified.  Its spin factors, like the float32 tier's, are float32
+// evaluations (the mixed-precision contract).
 template <int C, int P, bool WEIGHT>
 __device__ __forceinline__ bool df_sample(const ScatterArgs &a, int det, int t, const dfl (&qd)[4], float T,
                           float Pr, float det_wt, const int *mult, unsigned vmask) {
@@ -146,7 +148,7 @@ __device__ __forceinline__ bool df_sample(const ScatterArgs &a, int det, int t, 
     int pix[NT][3];
     float w[NT], pf[3];
     int n = 0;
-    if (!fast_pointing<C, P>(a.g, a.ft, a.fc, qb, qd, a.g.ncomp, T, Pr, pix, w, n, pf))
+    if (!fast_pointing<C, P, false>(a.g, a.ft, a.fc, qb, qd, a.g.ncomp, T, Pr, pix, w, n, pf))
         return false;
     const float sig = (!WEIGHT && n > 0) ? __ldg(a.signal + det * a.sig_stride + t) : 0.f;
     for (int k = 0; k < n; k++) {
