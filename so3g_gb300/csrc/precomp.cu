@@ -1,7 +1,9 @@
 // precomp.cu -- ProjEng_Precomp: projection with precomputed pointing
 // (pixel indices and spin projection factors per sample).  No trigonometry:
 // these kernels stream the pointing, the signal and the map and are bound by
-// HBM bandwidth and atomic throughput.
+// HBM bandwidth and atomic throughput.  Untiled maps over whole rows take
+// the vectorised kernels (k_pc_scatter4, k_pc_from_map4); everything else
+// the per-sample ones.
 
 #include "host.h"
 
@@ -213,6 +215,216 @@ __global__ void __launch_bounds__(kBlock) k_pc_from_map(PcArgs a) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Vectorised kernels for the common case: an untiled map, whole detector
+// rows (no sample ranges), n_time a multiple of 4 and 16-byte aligned
+// arrays.  Each thread takes 4 consecutive samples of its detector per
+// iteration and moves them with 16-byte loads: the pixel pairs as two
+// int4, the spin factors as NC float4, the signal as one float4 -- six
+// load instructions per 4 samples instead of five per sample, so that the
+// memory system, not the load issue rate, sets the pace.
+
+// Groups of 4 consecutive samples a thread of k_pc_scatter4 takes per
+// iteration (its runs of equal pixels are merged across them).
+constexpr int kPcGroups = 2;
+
+// The 4 samples' pixel pairs (iy, ix) and spin factors from sample index s
+// (a multiple of 4).
+template <int NC>
+__device__ __forceinline__ void pc_load4(const PcArgs &a, long long s, int (&p)[8],
+                                         float (&f)[4 * NC]) {
+    const int4 *pp = reinterpret_cast<const int4 *>(a.pixel) + (s >> 1);
+    const int4 u = __ldg(pp), v = __ldg(pp + 1);
+    p[0] = u.x; p[1] = u.y; p[2] = u.z; p[3] = u.w;
+    p[4] = v.x; p[5] = v.y; p[6] = v.z; p[7] = v.w;
+    const float4 *fp = reinterpret_cast<const float4 *>(a.spin + s * NC);
+#pragma unroll
+    for (int k = 0; k < NC; k++) {
+        const float4 w = __ldg(fp + k);
+        f[4 * k] = w.x; f[4 * k + 1] = w.y; f[4 * k + 2] = w.z; f[4 * k + 3] = w.w;
+    }
+}
+
+// Pixelizor2_Flat<NonTiled>::pix (src/Projection.cxx:881-886) for a
+// precomputed pair: the element offset, or -1 (iy < 0: skipped; out of
+// range: recorded).
+__device__ __forceinline__ long long pc_offset(const PcArgs &a, int iy, int ix, int det,
+                                               int t) {
+    if (iy < 0) return -1;
+    if (iy >= a.ny || ix < 0 || ix >= a.nx) {
+        record_pixel_range(a.err, 0, det, t);
+        return -1;
+    }
+    return (long long)iy * a.nx + ix;
+}
+
+// The thread's 4 * kPcGroups consecutive samples often share a pixel (a scan crosses a
+// pixel in several samples): their float32 terms are summed in registers
+// with compensated (TwoSum) additions and each run of equal pixels is
+// flushed with one float64 atomic per value -- hi + lo added in float64,
+// which is the exact run sum to ~2^-46, so the map differs from the
+// per-sample sums only in float64 summation order.  The L2 atomic rate,
+// not HBM, bounds the per-sample form of this kernel.
+template <int NV>
+__device__ __forceinline__ void pc_flush(double *map, long long off, long long plane,
+                                         const int (&slot)[NV], const float (&hi)[NV],
+                                         const float (&lo)[NV]) {
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+        double d = f2d(hi[k]);
+        if (lo[k] != 0.f) d += f2d(lo[k]);
+        atomicAdd(map + off + slot[k] * plane, d);
+    }
+}
+
+template <bool WEIGHT, int NC, int G = kPcGroups>
+__global__ void __launch_bounds__(kBlock) k_pc_scatter4(PcArgs a) {
+    constexpr int NV = WEIGHT ? NC * (NC + 1) / 2 : NC;
+    int det, t0, t1;
+    if (!seg_piece(a.segs, a.piece, det, t0, t1)) return;
+    float det_wt = 1.f;
+    if (a.det_weights) {
+        det_wt = __ldg(a.det_weights + det);
+        if (det_wt == 0.f) return;  // src/Projection.cxx:2101-2105
+    }
+    const long long plane = (long long)a.ny * a.nx;
+    // Value k goes to map plane slot[k]: component c (to_map) or the
+    // upper-triangle pair (i, j), j >= i, at i * NC + j (to_weight_map).
+    int slot[NV];
+    {
+        int k = 0;
+        if (!WEIGHT) {
+#pragma unroll
+            for (int c = 0; c < NC; c++) slot[k++] = c;
+        } else {
+#pragma unroll
+            for (int i = 0; i < NC; i++)
+#pragma unroll
+                for (int j = i; j < NC; j++) slot[k++] = i * NC + j;
+        }
+    }
+    for (int t = t0 + 4 * G * threadIdx.x; t < t1; t += 4 * G * blockDim.x) {
+        long long cur = -1;
+        float hi[NV], lo[NV];
+#pragma unroll
+        for (int g = 0; g < G; g++) {
+            const int tg = t + 4 * g;
+            if (tg >= t1) break;   // t1 - t0 is a multiple of 4 only
+            const long long s = (long long)det * a.n_time + tg;
+            int p[8];
+            float f[4 * NC];
+            pc_load4<NC>(a, s, p, f);
+            float4 sg = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (!WEIGHT)
+                sg = __ldg(reinterpret_cast<const float4 *>(a.signal + det * a.sig_stride + tg));
+            const float sig[4] = {sg.x, sg.y, sg.z, sg.w};
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const long long off = pc_offset(a, p[2 * j], p[2 * j + 1], det, tg + j);
+                if (off < 0) continue;
+                const float *pf = f + NC * j;
+                float v[NV];
+                if (!WEIGHT) {
+                    // src/Projection.cxx:2117
+#pragma unroll
+                    for (int c = 0; c < NC; c++) v[c] = det_wt * sig[j] * pf[c];
+                } else {
+                    // src/Projection.cxx:2151
+                    int k = 0;
+#pragma unroll
+                    for (int i = 0; i < NC; i++)
+#pragma unroll
+                        for (int m = i; m < NC; m++) v[k++] = pf[i] * pf[m] * det_wt;
+                }
+                if (off == cur) {
+#pragma unroll
+                    for (int k = 0; k < NV; k++) {
+                        float e;
+                        two_sum(hi[k], v[k], hi[k], e);
+                        lo[k] += e;
+                    }
+                } else {
+                    if (cur >= 0) pc_flush<NV>(a.map, cur, plane, slot, hi, lo);
+                    cur = off;
+#pragma unroll
+                    for (int k = 0; k < NV; k++) {
+                        hi[k] = v[k];
+                        lo[k] = 0.f;
+                    }
+                }
+            }
+        }
+        if (cur >= 0) pc_flush<NV>(a.map, cur, plane, slot, hi, lo);
+    }
+}
+
+template <int NC>
+__global__ void __launch_bounds__(kBlock) k_pc_from_map4(PcArgs a) {
+    // ProjEng_Precomp::from_map, src/Projection.cxx:2066-2082
+    int det, t0, t1;
+    if (!seg_piece(a.segs, a.piece, det, t0, t1)) return;
+    const long long plane = (long long)a.ny * a.nx;
+    for (int t = t0 + 4 * threadIdx.x; t < t1; t += 4 * blockDim.x) {
+        const long long s = (long long)det * a.n_time + t;
+        int p[8];
+        float f[4 * NC];
+        pc_load4<NC>(a, s, p, f);
+        float4 *sp = reinterpret_cast<float4 *>(a.signal_out + det * a.sig_stride + t);
+        const float4 sv = *sp;
+        float sig[4] = {sv.x, sv.y, sv.z, sv.w};
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const long long off = pc_offset(a, p[2 * j], p[2 * j + 1], det, t + j);
+            if (off < 0) continue;
+            const float *pf = f + NC * j;
+            // The reference sums the components into a float32 sig = 0 (each
+            // `sig += pf * map` a float64 product and sum rounded to
+            // float32: certified double-float roundings, fast_accum; the
+            // float64 arithmetic itself where one is uncertain), then adds
+            // sig to the signal.
+            double mv[NC];
+            float s1 = 0.f;
+            bool ok = true;
+#pragma unroll
+            for (int c = 0; c < NC; c++) {
+                mv[c] = __ldg(a.map + off + c * plane);
+                ok = ok && fast_accum(s1, mv[c], pf[c]);
+            }
+            if (!ok) {
+                s1 = 0.f;
+#pragma unroll
+                for (int c = 0; c < NC; c++) s1 += pf[c] * mv[c];
+            }
+            sig[j] += s1;
+        }
+        *sp = make_float4(sig[0], sig[1], sig[2], sig[3]);
+    }
+}
+
+// True when the vectorised kernels apply (see above).
+bool pc_vec_ok(const PcArgs &a, const void *sig, long long sig_stride, bool whole_rows) {
+    auto al = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
+    return !a.tiled && whole_rows && (a.n_time % 4) == 0 && al(a.pixel) && al(a.spin) &&
+           (!sig || (al(sig) && (sig_stride % 4) == 0));
+}
+
+template <bool WEIGHT>
+void pc_scatter4_launch(const PcArgs &a, dim3 grid, cudaStream_t st) {
+    switch (a.nc) {
+    case 1: k_pc_scatter4<WEIGHT, 1><<<grid, kBlock, 0, st>>>(a); break;
+    case 2: k_pc_scatter4<WEIGHT, 2><<<grid, kBlock, 0, st>>>(a); break;
+    default: k_pc_scatter4<WEIGHT, 3><<<grid, kBlock, 0, st>>>(a); break;
+    }
+}
+
+void pc_from_map4_launch(const PcArgs &a, dim3 grid, cudaStream_t st) {
+    switch (a.nc) {
+    case 1: k_pc_from_map4<1><<<grid, kBlock, 0, st>>>(a); break;
+    case 2: k_pc_from_map4<2><<<grid, kBlock, 0, st>>>(a); break;
+    default: k_pc_from_map4<3><<<grid, kBlock, 0, st>>>(a); break;
+    }
+}
+
 int pc_common(PcArgs &a, const so3g_precomp_geom *g, const int32_t *pixel,
               const float *spin_proj, int32_t n_det, int32_t n_time, const so3g_map *map) {
     clear_error();
@@ -271,7 +483,9 @@ int so3g_precomp_to_map(const so3g_precomp_geom *g, const int32_t *pixel,
     a.err = err;
     a.map = map->data;
     dim3 grid((unsigned)n_seg, (unsigned)((max_len + a.piece - 1) / a.piece));
-    if (a.tiled) k_pc_scatter<true, false><<<grid, kBlock, 0, (cudaStream_t)stream>>>(a);
+    if (pc_vec_ok(a, signal, sig_det_stride, !ranges))
+        pc_scatter4_launch<false>(a, grid, (cudaStream_t)stream);
+    else if (a.tiled) k_pc_scatter<true, false><<<grid, kBlock, 0, (cudaStream_t)stream>>>(a);
     else k_pc_scatter<false, false><<<grid, kBlock, 0, (cudaStream_t)stream>>>(a);
     return after_launch("precomp to_map");
 }
@@ -295,7 +509,9 @@ int so3g_precomp_to_weight_map(const so3g_precomp_geom *g, const int32_t *pixel,
     a.err = err;
     a.map = map->data;
     dim3 grid((unsigned)n_seg, (unsigned)((max_len + a.piece - 1) / a.piece));
-    if (a.tiled) k_pc_scatter<true, true><<<grid, kBlock, 0, (cudaStream_t)stream>>>(a);
+    if (pc_vec_ok(a, nullptr, 0, !ranges))
+        pc_scatter4_launch<true>(a, grid, (cudaStream_t)stream);
+    else if (a.tiled) k_pc_scatter<true, true><<<grid, kBlock, 0, (cudaStream_t)stream>>>(a);
     else k_pc_scatter<false, true><<<grid, kBlock, 0, (cudaStream_t)stream>>>(a);
     return after_launch("precomp to_weight_map");
 }
@@ -316,7 +532,9 @@ int so3g_precomp_from_map(const so3g_precomp_geom *g, const int32_t *pixel,
     a.err = err;
     a.map = map->data;
     dim3 grid((unsigned)n_det, (unsigned)((n_time + a.piece - 1) / a.piece));
-    if (a.tiled) k_pc_from_map<true><<<grid, kBlock, 0, (cudaStream_t)stream>>>(a);
+    if (pc_vec_ok(a, signal, sig_det_stride, true))
+        pc_from_map4_launch(a, grid, (cudaStream_t)stream);
+    else if (a.tiled) k_pc_from_map<true><<<grid, kBlock, 0, (cudaStream_t)stream>>>(a);
     else k_pc_from_map<false><<<grid, kBlock, 0, (cudaStream_t)stream>>>(a);
     return after_launch("precomp from_map");
 }

@@ -93,3 +93,49 @@ def test_precomp_pixel_out_of_range(orc, gpulib):
     proj = np.ones((1, 10, 3), np.float32)
     with pytest.raises(ValueError, match="out of range"):
         pe.to_map(np.zeros((3, 4, 5)), pix, proj, np.ones((1, 10), np.float32), None, None)
+
+
+@pytest.mark.parametrize("n_time", [3000, 3004, 3001])
+@pytest.mark.parametrize("ncomp", [1, 2, 3])
+def test_precomp_vector_and_scalar_paths(orc, gpulib, n_time, ncomp):
+    """n_time a multiple of 4 (16-byte aligned rows): the vectorised
+    kernels; otherwise the per-sample ones.  Both against the oracle: maps
+    to float64 summation order, from_map into a non-zero signal bit for bit,
+    with samples off the map (negative pixel) and detector weights."""
+    import torch
+    c = Case(orc, coord="CAR", ncomp=ncomp, tiled=False, n_det=6, n_time=n_time)
+    pix, proj = orc.pointing_matrix(c.pz, c.bore, c.dets, c.resp, c.eng.index_count)
+    pix[1, ::7, 0] = -1
+    pe = so3g_gb300.ProjEng_Precomp_NonTiled()
+    w = np.array([1., 0., 2., .5, 1.5, .25], np.float32)
+    m = c.blank((ncomp,))
+    naxis = m.shape[-2:]
+    want = np.zeros_like(m)
+    orc.precomp_to_map(pix, proj, c.signal, w, want, naxis=naxis)
+    got = pe.to_map(m, pix, proj, c.signal, w, None)
+    assert np.abs(got - want).max() <= 1e-12 * np.abs(want).max()
+    ww = np.zeros((ncomp,) + m.shape)
+    orc.precomp_to_weight_map(pix, proj, w, ww, naxis=naxis)
+    gw = pe.to_weight_map(np.zeros_like(ww), pix, proj, w, None)
+    assert np.abs(gw - ww).max() <= 1e-12 * np.abs(ww).max()
+    src = c.random_map((ncomp,))
+    sig0 = np.random.default_rng(3).standard_normal((6, n_time)).astype(np.float32)
+    want_s = sig0.copy()
+    orc.precomp_from_map(pix, proj, src, want_s, naxis=naxis)
+    got_s = np.array(pe.from_map(src, pix, proj, sig0.copy()))
+    assert bits_equal(got_s, want_s)
+    # Device tensors take the same kernels.
+    dev = [torch.from_numpy(x).cuda() for x in (pix, proj, sig0.copy())]
+    got_d = pe.from_map(torch.from_numpy(src).cuda(), *dev).cpu().numpy()
+    assert bits_equal(got_d, want_s)
+
+
+def test_precomp_pixel_out_of_range_vectorised(orc, gpulib):
+    pe = so3g_gb300.ProjEng_Precomp_NonTiled()
+    pix = np.zeros((2, 16, 2), np.int32)
+    pix[1, 5] = (4, 0)      # row 4 of a (3, 4, 5) map
+    proj = np.ones((2, 16, 3), np.float32)
+    with pytest.raises(ValueError, match="out of range"):
+        pe.to_map(np.zeros((3, 4, 5)), pix, proj, np.ones((2, 16), np.float32), None, None)
+    with pytest.raises(ValueError, match="out of range"):
+        pe.from_map(np.zeros((3, 4, 5)), pix, proj, None)
