@@ -112,6 +112,16 @@ __device__ __forceinline__ void load_bore_f32(const float4 *b32, const double *b
     }
 }
 
+// Reciprocal by the hardware approximation (PTX rcp.approx.ftz.f32, at most
+// 1 ulp = 2u relative error; subnormal inputs flush to zero, which the
+// callers exclude): one instruction, against the several of the correctly
+// rounded __frcp_rn.
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // Piecewise-linear table value in float32: knot i and fraction f of
 // u * (n-1); also returns the local slope (table units per unit of u).
 __device__ __forceinline__ float lut_f(const float4 *t, float u, float &slope) {
@@ -169,14 +179,16 @@ __device__ __forceinline__ bool mixed_lonlat(const FastTables &ft, const MixedCo
     const float ay = fabsf(Y), ax = fabsf(X);
     if (X < 0.f && !(ay > 64.f * kU)) return false;   // the +-pi seam
     const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
-    const float inv_mx = __frcp_rn(mx);
-    // r = mn * (1/mx) rounded twice (2u); atan has slope <= 1.
+    // mx >= |(X, Y)| / sqrt(2) > 0.15 here (|sin lat| < 0.9).
+    const float inv_mx = rcp_approx(mx);
+    // r = mn * (1/mx): the reciprocal's 2u and the product's u (3u);
+    // atan has slope <= 1.
     float slope_lon;
     const float th = lut_f(ft.atan2_t, mn * inv_mx, slope_lon);
     float lon = (ax < ay) ? mc.half_pi - th : th;
     if (X < 0.f) lon = mc.pi - lon;
     if (Y < 0.f) lon = -lon;
-    // lon error <= 22.9u / cos(lat) + 2u (r) + the table's roundings
+    // lon error <= 22.9u / cos(lat) + 3u (r) + the table's roundings
     // (u |th| + u |dv f| + u |th|, with |dv f| <= 1e-4: 2u |th| + 0.01u)
     // + 3.2u if th was subtracted from pi/2 + 6.3u if from pi (those
     // constants' roundings and the subtractions'), and 1 / cos(lat) <=
@@ -189,7 +201,7 @@ __device__ __forceinline__ bool mixed_lonlat(const FastTables &ft, const MixedCo
     o.lon = lon;
     o.lat = lat;
     o.elon = fmaf(11.5f * kU, inv_mx,
-                  fmaf(2.f * kU, th, (2.01f + (ax < ay ? 3.2f : 0.f) + (X < 0.f ? 6.3f : 0.f)) * kU));
+                  fmaf(2.f * kU, th, (3.01f + (ax < ay ? 3.2f : 0.f) + (X < 0.f ? 6.3f : 0.f)) * kU));
     o.elat = fmaf(slope_lat, fmaf(21.f * kU, fabsf(cos_t), 4.f * kU),
                   fmaf(2.f * kU, fabsf(lat), 20.11f * kU));
     return true;
@@ -206,8 +218,9 @@ __device__ __forceinline__ void mixed_spin(const MixedLonLat &o, int nc, float T
     }
     const float a = o.a, b = o.b, c = o.c, d = o.d;
     const float Nc = fmaf(a, c, -b * d), Ns = fmaf(c, d, a * b);
+    // D = (1 - sin^2 lat) / 4 > 0.04 where the float32 tier applies.
     const float D = fmaf(a, a, d * d) * fmaf(b, b, c * c);
-    const float k = Pr * __frcp_rn(D);
+    const float k = Pr * rcp_approx(D);
     const float v1 = fmaf(Nc, Nc, -Ns * Ns) * k, v2 = 2.f * Nc * Ns * k;
     if (nc == 2) {
         pf[0] = v1;
