@@ -429,6 +429,52 @@ int so3g_precomp_from_map(const so3g_precomp_geom *g,
                           float *signal, int64_t sig_det_stride,
                           int32_t *err, void *stream);
 
+/* ---- Boresight generation (the step before the path) --------------------- */
+
+/* Sight-line models of CelestialSightLine (python/proj/coords.py). */
+enum so3g_sight_kind {
+    SO3G_SIGHT_HORIZON    = 0,  /* for_horizon, coords.py:190-209 */
+    SO3G_SIGHT_NAIVE_AZEL = 1   /* naive_az_el, coords.py:99-125 */
+};
+
+/* Constants of a sight line, formed on the host as the Python layer forms
+ * them (so that both sides share their bits):
+ *   horizon:    Q = euler(2, -az) * euler(1, pi/2 - el) * euler(2, roll)
+ *   naive:      Q = euler(2, lst) * q_site_lat * q_pi * euler(2, -az)
+ *                   * euler(1, pi/2 - el) * euler(2, roll),
+ *               lst = (era_poly[0] * J + era_poly[1]) + site_lon_rad,
+ *               J = (t - era_epoch) / 86400
+ * each product taken left to right, as numpy evaluates the expression;
+ * then, with has_left, Q = q_left * Q (the Projectionist's
+ * q_celestial_to_native * Q, python/proj/wcs.py:140-148). */
+typedef struct so3g_sightline {
+    int32_t kind;            /* so3g_sight_kind */
+    int32_t has_left;        /* apply q_left */
+    double roll;             /* roll where the roll array is NULL */
+    double site_lon_rad;     /* naive: site.lon * DEG */
+    double era_epoch;        /* naive: ERA_EPOCH */
+    double era_poly[2];      /* naive: ERA_POLY */
+    double q_site_lat[4];    /* naive: euler(1, pi/2 - site.lat * DEG) */
+    double q_pi[4];          /* naive: euler(2, pi) */
+    double q_left[4];
+} so3g_sightline;
+
+/* Boresight quaternions q_out (n, 4) float64 of a sight line from the
+ * per-sample arrays t (naive only; NULL for horizon), az, el and roll
+ * (NULL: sl->roll), all (n,) float64 device arrays.  Replaces the numpy
+ * evaluation of CelestialSightLine.for_horizon / naive_az_el
+ * (python/proj/coords.py:99-125, 190-209) and, with has_left, the
+ * quat x G3VectorQuat product of Projectionist._cache_q_fp_to_native. */
+int so3g_boresight(const so3g_sightline *sl, const double *t, const double *az,
+                   const double *el, const double *roll, int64_t n, double *q_out,
+                   void *stream);
+
+/* q_out[i] = q_left * q_in[i] for n quaternions (device arrays (n, 4)
+ * float64; q_left host, 4 float64): spt3g's quat x G3VectorQuat product,
+ * used by Projectionist._cache_q_fp_to_native (python/proj/wcs.py:140-148). */
+int so3g_quat_left_multiply(const double *q_left, const double *q_in, int64_t n,
+                            double *q_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -86,6 +86,23 @@ class Obs(ctypes.Structure):
     ]
 
 
+class SightLine(ctypes.Structure):
+    _fields_ = [
+        ("kind", c_int32),
+        ("has_left", c_int32),
+        ("roll", c_double),
+        ("site_lon_rad", c_double),
+        ("era_epoch", c_double),
+        ("era_poly", c_double * 2),
+        ("q_site_lat", c_double * 4),
+        ("q_pi", c_double * 4),
+        ("q_left", c_double * 4),
+    ]
+
+
+# enum so3g_sight_kind
+SIGHT_HORIZON, SIGHT_NAIVE_AZEL = 0, 1
+
 P = ctypes.POINTER
 _SIGS = {
     "so3g_init": (ctypes.c_int, []),
@@ -136,6 +153,10 @@ _SIGS = {
     "so3g_precomp_from_map": (ctypes.c_int, [P(PrecompGeom), c_void_p, c_void_p, c_int32,
                                              c_int32, P(Map), c_void_p, c_int64, c_void_p,
                                              c_void_p]),
+    "so3g_boresight": (ctypes.c_int, [P(SightLine), c_void_p, c_void_p, c_void_p, c_void_p,
+                                      c_int64, c_void_p, c_void_p]),
+    "so3g_quat_left_multiply": (ctypes.c_int, [c_void_p, c_void_p, c_int64, c_void_p,
+                                               c_void_p]),
 }
 
 _lib = None

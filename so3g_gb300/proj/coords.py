@@ -39,6 +39,14 @@ ERA_EPOCH = 946684800 + 3600 * 12
 ERA_POLY = np.array([6.300387486754831, 4.894961212823756])
 
 
+def _on_device(*xs):
+    """True if any argument is a CUDA torch tensor (torch imported only when
+    one could be)."""
+    import sys
+    torch = sys.modules.get("torch")
+    return torch is not None and any(isinstance(x, torch.Tensor) and x.is_cuda for x in xs)
+
+
 class CelestialSightLine:
     """A vector of boresight pointing quaternions, in ``self.Q``."""
 
@@ -58,6 +66,11 @@ class CelestialSightLine:
         Earth rotation angle only (python/proj/coords.py:99-125)."""
         site = cls.decode_site(site)
         self = cls()
+        if _on_device(t, az, el, roll):
+            # CUDA tensors in: the boresight is formed on the device.
+            from .. import sightline
+            self.Q = sightline.boresight("naive", t, az, el, roll, site=site)
+            return self
         J = (np.asarray(t) - ERA_EPOCH) / 86400
         era = np.polyval(ERA_POLY, J)
         lst = era + site.lon * DEG
@@ -88,6 +101,11 @@ class CelestialSightLine:
         """Local horizon coordinates taken as "celestial"
         (python/proj/coords.py:190-209)."""
         self = cls()
+        if _on_device(az, el, roll):
+            # CUDA tensors in: the boresight is formed on the device.
+            from .. import sightline
+            self.Q = sightline.boresight("horizon", t, az, el, roll)
+            return self
         az, el, t = map(np.asarray, [az, el, t])
         roll = 0. if roll is None else np.asarray(roll)
         self.Q = (quat.euler(2, -az) * quat.euler(1, np.pi / 2 - el) * quat.euler(2, roll))

@@ -71,7 +71,14 @@ class _ProjectionistBase:
 
     def _cache_q_fp_to_native(self, q_fp_to_celestial):
         if q_fp_to_celestial is not self._q_fp_to_celestial:
-            self._q_fp_to_native = self.q_celestial_to_native * q_fp_to_celestial
+            from .coords import _on_device
+            if _on_device(q_fp_to_celestial):
+                # A boresight held on the device: the product runs there.
+                from .. import sightline
+                self._q_fp_to_native = sightline.left_multiply(self.q_celestial_to_native,
+                                                               q_fp_to_celestial)
+            else:
+                self._q_fp_to_native = self.q_celestial_to_native * q_fp_to_celestial
             self._q_fp_to_celestial = q_fp_to_celestial
         return self._q_fp_to_native
 

@@ -59,7 +59,8 @@ def test_struct_layout_matches_header(tmp_path):
     from so3g_gb300 import _abi
     import ctypes
     structs = {"so3g_pixelization": _abi.Pixelization, "so3g_map": _abi.Map,
-               "so3g_ranges": _abi.Ranges, "so3g_precomp_geom": _abi.PrecompGeom, "so3g_obs": _abi.Obs}
+               "so3g_ranges": _abi.Ranges, "so3g_precomp_geom": _abi.PrecompGeom, "so3g_obs": _abi.Obs,
+               "so3g_sightline": _abi.SightLine}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "so3g_gb300.h"',
              'int main(void) {']
     for cname, py in structs.items():
