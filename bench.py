@@ -73,6 +73,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64-path", action="store_true")
+    ap.add_argument("--no-precomp", action="store_true",
+                    help="leave out the precomputed-pointing leg of the default line")
     ap.add_argument("--ops", default="to_map,from_map",
                     help="operations timed in a step (profiling runs pick one)")
     ap.add_argument("--batch-scale", type=float, default=1.0,
@@ -507,9 +509,11 @@ def run_e2e(args, c, eng, q, dets, resp, sig_dev, dev):
 # ---------------------------------------------------------------------------
 # Precomputed pointing: ProjEng_Precomp on the workload's pointing matrix.
 
-def run_precomp(args, c):
-    """One step = Precomp to_map + from_map over all samples, the pixel
-    indices and spin factors computed once beforehand (pointing_matrix)."""
+def precomp_leg(c, steps, warmup):
+    """ProjEng_Precomp to_map + from_map on the workload's precomputed
+    pointing (pixel indices and spin factors from pointing_matrix, computed
+    once and timed on its own): the form a map-maker iterating over the same
+    observation uses.  Returns the timings and the HBM roofline."""
     import torch
     import so3g_gb300
     from so3g_gb300 import _abi
@@ -519,13 +523,21 @@ def run_precomp(args, c):
     p, q, dets, resp = host_inputs(c)
     eng = p.get_ProjEng("TQU")
     q_d, dets_d, resp_d = (torch.from_numpy(x).to(dev) for x in (q, dets, resp))
+    stream = torch.cuda.current_stream()
+    eng.pointing_matrix(q_d, dets_d, resp_d)    # warm-up
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
     pix, spin = eng.pointing_matrix(q_d, dets_d, resp_d)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    pm_ms = e0.elapsed_time(e1)
     del q_d
     sig = make_signal(torch, c, dev)
     pc = so3g_gb300.ProjEng_Precomp_NonTiled()
     m = torch.zeros((3,) + tuple(c["shape"]), dtype=torch.float64, device=dev)
     out = torch.zeros_like(sig)
-    stream = torch.cuda.current_stream()
     N = c["n_det"] * c["n_time"]
 
     def step(ev):
@@ -538,7 +550,7 @@ def run_precomp(args, c):
         pc.from_map(m, pix, spin, out)
         ev[3].record(stream)
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step([torch.cuda.Event(enable_timing=True) for _ in range(4)])
     torch.cuda.synchronize()
     n0 = lib.so3g_launch_count()
@@ -547,14 +559,14 @@ def run_precomp(args, c):
     e1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev.index) as clk:
         e0.record(stream)
-        for _ in range(args.steps):
+        for _ in range(steps):
             ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
             step(ev)
             evs.append(ev)
         e1.record(stream)
         torch.cuda.synchronize()
     launches = lib.so3g_launch_count() - n0
-    ms = e0.elapsed_time(e1) / args.steps
+    ms = e0.elapsed_time(e1) / steps
     tm = float(np.mean([a.elapsed_time(b) for a, b, _, _ in evs]))
     fm = float(np.mean([a.elapsed_time(b) for _, _, a, b in evs]))
     npix = c["shape"][0] * c["shape"][1]
@@ -565,23 +577,32 @@ def run_precomp(args, c):
     hbm, kind = peaks()
     ach_tm = b_tm * N / (tm * 1e-3) / 1e9
     ach_fm = b_fm * N / (fm * 1e-3) / 1e9
-    metric, workload, map_shape = describe(c)
-    line = {"metric": "Precomp to_map/from_map TOD samples/s (CAR TQU, precomputed pointing)",
-            "value": N / (ms * 1e-3), "unit": "samples/s", "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": workload + ", pointing precomputed (ProjEng_Precomp)",
-                       "n_det": c["n_det"], "n_time": c["n_time"], "map": map_shape,
-                       "step": "Precomp to_map + from_map",
-                       "l2": "inputs larger than L2 (pointing + TOD %.1f GB)" % (N * 24 / 1e9),
-                       "parallelism": "single GPU"},
-            "op_ms": {"to_map": tm, "from_map": fm},
+    del pix, spin, sig, out, m
+    return {"value": N / (ms * 1e-3), "ms_per_step": ms, "op_ms": {"to_map": tm, "from_map": fm},
+            "pointing_matrix_ms": pm_ms,
             "roofline": {"bound": "hbm", "kernel": "precomp from_map", "achieved": ach_fm,
                          "peak": hbm, "unit": "GB/s", "frac": ach_fm / hbm, "traffic": None,
                          "bytes_per_sample": b_fm, "peak_kind": kind,
                          "to_map": {"achieved": ach_tm, "frac": ach_tm / hbm,
                                     "bytes_per_sample": b_tm}},
             "clocks": clk.summary(), "gpu_launches": int(launches)}
+
+
+def run_precomp(args, c):
+    r = precomp_leg(c, args.steps, args.warmup)
+    N = c["n_det"] * c["n_time"]
+    metric, workload, map_shape = describe(c)
+    line = {"metric": "Precomp to_map/from_map TOD samples/s (CAR TQU, precomputed pointing)",
+            "value": r["value"], "unit": "samples/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": workload + ", pointing precomputed (ProjEng_Precomp)",
+                       "n_det": c["n_det"], "n_time": c["n_time"], "map": map_shape,
+                       "step": "Precomp to_map + from_map",
+                       "l2": "inputs larger than L2 (pointing + TOD %.1f GB)" % (N * 24 / 1e9),
+                       "parallelism": "single GPU"},
+            "op_ms": r["op_ms"], "pointing_matrix_ms": r["pointing_matrix_ms"],
+            "roofline": r["roofline"], "clocks": r["clocks"], "gpu_launches": r["gpu_launches"]}
     print(json.dumps(line))
 
 
@@ -882,6 +903,17 @@ def main():
                                  "samples_per_s": N / (res["to_weight_map_ms"] * 1e-3)}
     if "e2e" in res:
         line["e2e"] = res["e2e"]
+    if world == 1 and c["kind"] == "car" and not args.no_precomp:
+        # The same workload with its pointing precomputed once
+        # (ProjEng_Precomp): the HBM-bound form of the path.
+        r = precomp_leg(c, args.steps, args.warmup)
+        line["precomp"] = {"value": r["value"], "unit": "samples/s",
+                           "ms_per_step": r["ms_per_step"], "op_ms": r["op_ms"],
+                           "pointing_matrix_ms": r["pointing_matrix_ms"],
+                           "roofline": r["roofline"], "gpu_launches": r["gpu_launches"],
+                           "step": "Precomp to_map + from_map on pointing_matrix output "
+                                   "(pixel indices bit-exact, spin factors as the "
+                                   "certified path)"}
     if world == 1 and not args.no_cpu:
         nd, nt = cpu_sample_size(c)
         r = run_cpu(c, nd, nt)

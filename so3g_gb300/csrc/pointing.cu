@@ -30,6 +30,9 @@ struct PointArgs {
     long long max_edges;
     unsigned long long *n_edges;
     int *err;
+    int fast;               // certified pointing for pixels()/pointing_matrix()
+    FastTables ft;
+    FastConst fc;
 };
 
 // ---- coords ---------------------------------------------------------------
@@ -56,6 +59,66 @@ __global__ void __launch_bounds__(kBlock) k_coords(PointArgs a) {
 // precede the first complete tuple of their sub-range get kSentinel, which
 // k_pixels_fix then replaces with the tuple carried from earlier sub-ranges.
 
+// Pixelizations whose pixels() / pointing_matrix() use the certified
+// double-float pointing.
+template <int C, int P>
+struct PixCert {
+    static constexpr bool value =
+        (P == PX_HP_NT || P == PX_HP_T)
+            ? C == SO3G_COORD_CAR
+            : (C == SO3G_COORD_CAR || C == SO3G_COORD_TAN || C == SO3G_COORD_ZEA ||
+               C == SO3G_COORD_SIN);
+};
+
+// GetPixel of one sample (and, with PROJ, its spin factors) through the
+// certified double-float pointing; false when a decision or a spin factor
+// is not certain, and the caller takes the exact path.  GetPixel is the
+// nearest pixel with [0, n) bounds for every flat pixelizor, interpolating
+// or not, tiled or not (:845-863, :1029-1051): the NonTiled nearest pixel
+// is certified and the tile tuple formed from it.
+template <int C, int P, bool PROJ>
+__device__ __forceinline__ bool cert_pixel(const PointArgs &a, const dfl (&qb)[4],
+                                           const dfl (&qd)[4], int nc, float T, float Pr,
+                                           int *idx, bool &full, float *pf) {
+    dfl Nc, Ns, D;
+    int pix[1][3];
+    float w[4];
+    int n = 0;
+    if (P == PX_HP_NT || P == PX_HP_T) {
+        dfl qa, qb2, qc, qd2;
+        df_qmul(qb, qd, qa, qb2, qc, qd2);
+        const dfl cos_t = df_dot<4>({qa, qb2, qc, qd2}, {qa, df_neg(qb2), df_neg(qc), qd2});
+        if (!(fabsf(cos_t.hi) < 0.998f)) return false;
+        dfl lon;
+        if (!fast_lon_spin(a.ft, a.fc, qa, qb2, qc, qd2, cos_t, lon, Nc, Ns, D)) return false;
+        if (!fast_healpix<P>(a.g, a.ft, a.fc, cos_t, lon, pix, n) || n != 1) return false;
+        idx[0] = pix[0][0];
+        if (P == PX_HP_T) idx[1] = pix[0][1];
+        full = true;
+    } else {
+        dfl X, Y;
+        if (!fast_native<C>(a.ft, a.fc, qb, qd, X, Y, Nc, Ns, D)) return false;
+        const dfl x = df_add(df_mul(X, a.fc.inv_cdx), a.fc.off_x);
+        const dfl y = df_add(df_mul(Y, a.fc.inv_cdy), a.fc.off_y);
+        if (!fast_pixels<PX_FLAT_NT_NN>(a.g, x, y, pix, w, n)) return false;
+        full = n > 0;
+        if (!full) {
+            idx[0] = -1;
+        } else if (P == PX_FLAT_NT_NN || P == PX_FLAT_NT_BL) {
+            idx[0] = pix[0][0];
+            idx[1] = pix[0][1];
+        } else {
+            const int iy = pix[0][0], ix = pix[0][1];
+            const int sub_y = iy / a.g.ty, sub_x = ix / a.g.tx;
+            idx[0] = sub_y * a.g.ntx + sub_x;
+            idx[1] = iy - sub_y * a.g.ty;
+            idx[2] = ix - sub_x * a.g.tx;
+        }
+    }
+    if (PROJ) return fast_spin<true>(nc, T, Pr, Nc, Ns, D, pf);
+    return true;
+}
+
 template <int C, int P, bool PROJ>
 __global__ void __launch_bounds__(kBlock) k_pixels(PointArgs a, int sub) {
     constexpr int IC = PixTraits<P>::index_count;
@@ -71,6 +134,13 @@ __global__ void __launch_bounds__(kBlock) k_pixels(PointArgs a, int sub) {
     int carry[IC];
 #pragma unroll
     for (int j = 0; j < IC; j++) carry[j] = kSentinel;
+    dfl qd[4];
+    if (PixCert<C, P>::value && a.fast) {
+        qd[0] = df_of(ofs.a);
+        qd[1] = df_of(ofs.b);
+        qd[2] = df_of(ofs.c);
+        qd[3] = df_of(ofs.d);
+    }
     for (int base = (int)s0; base < s1; base += 32) {
         const int t = base + lane;
         const bool live = t < s1;
@@ -78,10 +148,30 @@ __global__ void __launch_bounds__(kBlock) k_pixels(PointArgs a, int sub) {
 #pragma unroll
         for (int j = 0; j < IC; j++) idx[j] = kSentinel;
         bool full = false;
-        double c[4];
+        float pf[3] = {0.f, 0.f, 0.f};
         if (live) {
-            get_coords<C>(a.g.lut, load_quat(a.bore + 4LL * t), ofs, c);
-            full = get_pixel<P>(a.g, c, idx);
+            bool done = false;
+            if constexpr (PixCert<C, P>::value) {
+                if (a.fast) {
+                    const double2 lo = __ldg(reinterpret_cast<const double2 *>(a.bore + 4LL * t));
+                    const double2 hi =
+                        __ldg(reinterpret_cast<const double2 *>(a.bore + 4LL * t) + 1);
+                    dfl qb[4];
+                    done = df_split(lo.x, qb[0]) & df_split(lo.y, qb[1]) &
+                           df_split(hi.x, qb[2]) & df_split(hi.y, qb[3]);
+                    done = done && cert_pixel<C, P, PROJ>(a, qb, qd, nc, T, Pr, idx, full, pf);
+                }
+            }
+            if (!done) {
+                // The exact float64 path: the pixelizations above for the
+                // few samples the certified pointing leaves, all others.
+#pragma unroll
+                for (int j = 0; j < IC; j++) idx[j] = kSentinel;
+                double c[4];
+                get_coords<C>(a.g.lut, load_quat(a.bore + 4LL * t), ofs, c);
+                full = get_pixel<P>(a.g, c, idx);
+                if (PROJ) spin_factors(nc, c, T, Pr, pf);
+            }
         }
         const unsigned vm = __ballot_sync(kFull, live && full);
         const unsigned before = vm & ((1u << lane) - 1u);
@@ -101,8 +191,6 @@ __global__ void __launch_bounds__(kBlock) k_pixels(PointArgs a, int sub) {
 #pragma unroll
             for (int j = 0; j < IC; j++) out[j] = idx[j];
             if (PROJ) {
-                float pf[3];
-                spin_factors(nc, c, T, Pr, pf);
                 float *pout = a.proj + ((long long)det * a.n_time + t) * nc;
 #pragma unroll
                 for (int k = 0; k < 3; k++)
@@ -294,6 +382,9 @@ int point_common(PointLaunch &L, const so3g_pixelization *pz, const double *bore
     L.stream = (cudaStream_t)stream;
     L.what = what;
     L.n_det = n_det;
+    L.a.ft = device_fast_tables();
+    L.a.fc = make_fast_const(L.a.g);
+    L.a.fast = fast_mode(pz, L.a.ft) != SO3G_POINTING_EXACT;
     return SO3G_OK;
 }
 

@@ -406,3 +406,84 @@ def test_certified_octant_boundaries():
     eng2 = type(eng)((200, 400, 0.9 * np.pi / 180, -0.9 * np.pi / 180, 100.5, 200.5))
     res = _compare(eng2, q, dets, resp, False, 3)
     assert (res[0] > 0).mean() > 0.9
+
+
+def _np(x):
+    """A result (tensor, array or list of per-detector rows) as one array."""
+    if isinstance(x, (list, tuple)):
+        return np.stack([_np(e) for e in x])
+    if hasattr(x, "cpu"):
+        return x.cpu().numpy()
+    return np.asarray(x)
+
+
+def _edge_quats(orc, eng, proj, n, seed):
+    """Native pointings on pixel edges (0, +-1e-13, 1e-9 and mid-pixel),
+    the map's outer edges and the x in (-1, 0) strip, with polarisation
+    angles where a spin factor vanishes (zenithal projections: solved for
+    those pixel coordinates by Newton's method)."""
+    rng = np.random.default_rng(seed)
+    ny, nx, dy, dx, cry, crx = eng.naxis + eng.cdelt + eng.crpix
+    ix = rng.integers(-2, nx + 2, n).astype(float)
+    iy = rng.integers(-2, ny + 2, n).astype(float)
+    jit = rng.choice([0., 1e-13, -1e-13, 1e-9, 0.5, -0.5], n)
+    gam = rng.choice([0., np.pi / 4, np.pi / 2, -np.pi / 4], n) + \
+        rng.choice([0., 1e-9, rng.uniform(0, np.pi)], n)
+    if proj == "CAR":
+        lon = (ix + jit - crx + 1 - 0.5) * dx
+        lat = (iy + jit - cry + 1 - 0.5) * dy
+    else:
+        u = (ix + jit - (crx - 0.5)) * abs(dx)
+        v = (iy + jit - (cry - 0.5)) * dy
+        lon, lat = _solve_lonlat(orc, eng, ix + jit, iy + jit, np.arctan2(u, v),
+                                 np.pi / 2 - np.hypot(u, v), gam)
+    return _quats_at(lon, lat, gam)
+
+
+@pytest.mark.parametrize("proj", ["CAR", "TAN", "ZEA", "SIN"])
+@pytest.mark.parametrize("tiled,interpol", [(False, None), (True, None), (False, "bilinear"),
+                                            (True, "bilinear")])
+def test_certified_pixels_and_pointing_matrix(orc, proj, tiled, interpol):
+    """pixels() and pointing_matrix() take the certified pointing (GetPixel
+    of every flat pixelizor is the [0, n)-bounded nearest pixel, spin
+    factors certified): bit-identical to the exact path on edge inputs,
+    including the stale slots of off-map samples."""
+    import torch
+    p, eng = _engine((300, 400), 0.5 * ARCMIN, tiled, proj=proj, interpol=interpol)
+    q = _edge_quats(orc, eng, proj, 30000, 21)
+    dets = np.array([[1., 0., 0., 0.], [np.cos(0.3), 0., 0., np.sin(0.3)]])
+    resp = np.array([[1., 1.], [0.7, 0.45]], np.float32)
+    qd, dd, rd = (torch.from_numpy(x).cuda() for x in (q, dets, resp))
+    out = {}
+    for mode in (_abi.POINTING_EXACT, _abi.POINTING_CERTIFIED):
+        eng.pointing = mode
+        pix = eng.pixels(qd, dd, None)
+        pm_pix, pm_proj = eng.pointing_matrix(qd, dd, rd, None, None)
+        out[mode] = [_np(x) for x in (pix, pm_pix, pm_proj)]
+    for a, b in zip(out[_abi.POINTING_EXACT], out[_abi.POINTING_CERTIFIED]):
+        assert bits_equal(a, b)
+    # The inputs do land off the map and on it.
+    assert (out[_abi.POINTING_EXACT][0][..., 0] == -1).any()
+    assert (out[_abi.POINTING_EXACT][0][..., 0] >= 0).any()
+
+
+@pytest.mark.parametrize("nest,tiled", [(False, False), (True, False), (True, True)])
+def test_certified_healpix_pointing_matrix(nest, tiled):
+    import torch
+    rng = np.random.default_rng(44)
+    n = 30000
+    z = rng.choice([2 / 3, -2 / 3], n) + rng.choice([0., 1e-15, -1e-15, 1e-12, 0.3], n)
+    lat = np.arcsin(np.clip(z, -1, 1))
+    lon = rng.uniform(-np.pi, np.pi, n)
+    q = _quats_at(lon, lat, rng.uniform(0, np.pi, n))
+    dets = np.array([[1., 0., 0., 0.]])
+    resp = np.ones((1, 2), np.float32)
+    p, eng = _hp_engine(256, nest, tiled)
+    qd, dd, rd = (torch.from_numpy(x).cuda() for x in (q, dets, resp))
+    out = {}
+    for mode in (_abi.POINTING_EXACT, _abi.POINTING_CERTIFIED):
+        eng.pointing = mode
+        pm_pix, pm_proj = eng.pointing_matrix(qd, dd, rd, None, None)
+        out[mode] = [_np(x) for x in (pm_pix, pm_proj)]
+    for a, b in zip(out[_abi.POINTING_EXACT], out[_abi.POINTING_CERTIFIED]):
+        assert bits_equal(a, b)
