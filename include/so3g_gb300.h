@@ -475,6 +475,24 @@ int so3g_boresight(const so3g_sightline *sl, const double *t, const double *az,
 int so3g_quat_left_multiply(const double *q_left, const double *q_in, int64_t n,
                             double *q_out, void *stream);
 
+/* ---- Cut masks to sample segments ----------------------------------------- */
+
+/* RangesMatrix.from_mask (python/proj/ranges.py:11-297; Ranges built from a
+ * boolean mask, src/Ranges.cxx) for an (n_det, n_time) uint8 mask in
+ * device memory (nonzero = sample in a range; row d at mask + d *
+ * det_stride): counts[d] = the number of runs of set samples in row d
+ * (device int32 array of n_det). */
+int so3g_mask_count_segments(const uint8_t *mask, int32_t n_det, int32_t n_time,
+                             int64_t det_stride, int32_t *counts, void *stream);
+
+/* Writes the runs as so3g_ranges segments: seg (3 int32 per segment, device)
+ * receives (d, start, end) for the runs of row d from index first[d] on,
+ * first being the exclusive prefix sum of counts (device int64, n_det);
+ * *max_len (device int32, zeroed by the caller) becomes the longest run. */
+int so3g_mask_fill_segments(const uint8_t *mask, int32_t n_det, int32_t n_time,
+                            int64_t det_stride, const int64_t *first, const int32_t *counts,
+                            int32_t *seg, int32_t *max_len, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -157,6 +157,10 @@ _SIGS = {
                                       c_int64, c_void_p, c_void_p]),
     "so3g_quat_left_multiply": (ctypes.c_int, [c_void_p, c_void_p, c_int64, c_void_p,
                                                c_void_p]),
+    "so3g_mask_count_segments": (ctypes.c_int, [c_void_p, c_int32, c_int32, c_int64, c_void_p,
+                                                c_void_p]),
+    "so3g_mask_fill_segments": (ctypes.c_int, [c_void_p, c_int32, c_int32, c_int64, c_void_p,
+                                               c_void_p, c_void_p, c_void_p, c_void_p]),
 }
 
 _lib = None

@@ -304,6 +304,9 @@ class _Signal:
 # ---------------------------------------------------------------------------
 # Thread intervals (derive_ranges, src/Projection.cxx:1856-1922).
 
+from .ranges import DeviceRangesMatrix  # noqa: E402
+
+
 def _is_ranges(x):
     return isinstance(x, RangesInt32)
 
@@ -356,12 +359,25 @@ def flatten_ranges(bunches):
 
 
 class _DevRanges:
-    """so3g_ranges for a thread_intervals argument (None = all samples)."""
+    """so3g_ranges for a thread_intervals argument (None = all samples; a
+    DeviceRangesMatrix is used where its segments lie)."""
 
     def __init__(self, thread_intervals, n_det, n_time):
-        bunches = derive_ranges(thread_intervals, n_det, n_time)
         self.struct = None
         self.seg_host = None
+        self.dev_seg = None
+        self.given = thread_intervals is not None
+        if isinstance(thread_intervals, DeviceRangesMatrix):
+            ti = thread_intervals
+            if ti.shape[0] != n_det:
+                raise shape_error("thread_intervals", "Expected RangesMatrix with n_det=%d but "
+                                  "encountered n_det=%d" % (n_det, ti.shape[0]))
+            if ti.shape[1] != n_time:
+                raise shape_error("thread_intervals", "Expected RangesMatrix with n_time=%d "
+                                  "but encountered n_time=%d" % (n_time, ti.shape[1]))
+            self.dev_seg = ti
+            return
+        bunches = derive_ranges(thread_intervals, n_det, n_time)
         if bunches is None:
             return
         seg, _, _ = flatten_ranges(bunches)
@@ -373,6 +389,15 @@ class _DevRanges:
         self.seg_host = np.ascontiguousarray(seg[seg[:, 2] > seg[:, 1]])
 
     def upload(self):
+        if self.dev_seg is not None:
+            d = self.dev_seg
+            self.seg = d.seg.to(_device()).contiguous()
+            s = _abi.Ranges()
+            s.seg = self.seg.data_ptr() if d.n_seg else None
+            s.n_seg = d.n_seg
+            s.max_len = d.max_len
+            self.struct = s
+            return self
         seg = self.seg_host
         if seg is None:
             return self
@@ -980,7 +1005,7 @@ class ProjEngBase:
         err = _ErrRecord()
         lib, pz = _abi.lib(), self._pz()
         acc = DEFAULT_ACCUM if accum is None else accum
-        host = _host_matrix(sig) if rng.seg_host is None else None
+        host = _host_matrix(sig) if not rng.given else None
         if host is not None:
             def launch(d0, d1, buf):
                 _abi.check(lib.so3g_proj_to_map(

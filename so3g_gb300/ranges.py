@@ -278,10 +278,95 @@ class RangesMatrix:
 
     @classmethod
     def from_mask(cls, mask):
+        if _is_cuda(mask) and mask.dim() == 2:
+            return DeviceRangesMatrix.from_mask(mask)
         mask = np.asarray(mask, dtype=bool)
         if mask.ndim == 1:
             return RangesInt32.from_mask(mask)
         return cls([cls.from_mask(m) for m in mask], child_shape=mask.shape[1:])
+
+
+def _is_cuda(x):
+    import sys
+    torch = sys.modules.get("torch")
+    return torch is not None and isinstance(x, torch.Tensor) and x.is_cuda
+
+
+class DeviceRangesMatrix:
+    """An (n_det, n_time) RangesMatrix held on the device as (det, start,
+    end) segments, built from a CUDA mask by RangesMatrix.from_mask
+    (so3g_mask_count_segments / so3g_mask_fill_segments) without a trip to
+    the host.  Passed as thread_intervals (one thread, a RangesMatrix
+    (ndet) in the reference's terms) its segments go to the projection
+    kernels where they lie; to_host() gives the RangesMatrix itself."""
+
+    def __init__(self, seg, n_det, n_time, max_len):
+        self.seg = seg              # (n_seg, 3) int32 CUDA tensor
+        self.n_seg = int(seg.shape[0])
+        self.max_len = int(max_len)
+        self._shape = (int(n_det), int(n_time))
+
+    @classmethod
+    def from_mask(cls, mask):
+        import torch
+        from . import _abi
+        from .projeng import _stream
+        if mask.dim() != 2:
+            raise ValueError("expected an (n_det, n_time) mask, got shape %s"
+                             % (tuple(mask.shape),))
+        dev = mask.device
+        with torch.cuda.device(dev):
+            m = mask
+            if m.dtype != torch.bool and m.dtype != torch.uint8:
+                m = m != 0
+            if m.stride(1) != 1:
+                m = m.contiguous()
+            m8 = m.view(torch.uint8) if m.dtype == torch.bool else m
+            n_det, n_time = m8.shape
+            lib, st = _abi.lib(), _stream()
+            counts = torch.zeros(n_det, dtype=torch.int32, device=dev)
+            _abi.check(lib.so3g_mask_count_segments(m8.data_ptr(), n_det, n_time, m8.stride(0),
+                                                    counts.data_ptr(), st),
+                       "mask_count_segments")
+            first = torch.cumsum(counts, 0, dtype=torch.int64) - counts
+            n_seg = int(counts.sum()) if n_det else 0
+            seg = torch.empty((n_seg, 3), dtype=torch.int32, device=dev)
+            max_len = torch.zeros(1, dtype=torch.int32, device=dev)
+            if n_seg:
+                _abi.check(lib.so3g_mask_fill_segments(m8.data_ptr(), n_det, n_time,
+                                                       m8.stride(0), first.data_ptr(),
+                                                       counts.data_ptr(), seg.data_ptr(),
+                                                       max_len.data_ptr(), st),
+                           "mask_fill_segments")
+            return cls(seg, n_det, n_time, int(max_len.item()))
+
+    @property
+    def shape(self):
+        return self._shape
+
+    def __len__(self):
+        return self._shape[0]
+
+    def __repr__(self):
+        return "DeviceRangesMatrix(%d,%d; %d segments)" % (self._shape + (self.n_seg,))
+
+    def to_host(self):
+        """The same ranges as a (host) RangesMatrix."""
+        seg = self.seg.cpu().numpy()
+        n_det, n_time = self._shape
+        rows = [RangesInt32(n_time) for _ in range(n_det)]
+        for d, a, b in seg:
+            rows[int(d)].append_interval_no_check(int(a), int(b))
+        return RangesMatrix(rows, child_shape=(n_time,))
+
+    def mask(self, dest=None):
+        return self.to_host().mask(dest)
+
+    def __getitem__(self, index):
+        return self.to_host()[index]
+
+    def __iter__(self):
+        return iter(self.to_host())
 
 
 def wrap_ivals(ivals):
