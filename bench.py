@@ -277,9 +277,12 @@ class ClockSampler:
 MEASURED_TRAFFIC_PER_SAMPLE = {
     "certified": {"to_map": (834.33e6 + 3.78e6) / 2e8,
                   "from_map": (835.40e6 + 747.14e6) / 2e8},
-    "mixed": {"to_map": (907.08e6 + 125.03e6) / 2e8,
-              "from_map": (894.75e6 + 860.11e6) / 2e8},
+    "mixed": {"to_map": (883.75e6 + 110.41e6) / 2e8,
+              "from_map": (859.73e6 + 844.40e6) / 2e8},
 }
+# The same for the Precomp kernels (ncu, 100 detectors x 1M samples).
+MEASURED_TRAFFIC_PRECOMP = {"to_map": (2.400763e9 + 3.709e6) / 1e8,
+                            "from_map": (2.406085e9 + 413.98e6) / 1e8}
 
 
 def algorithmic_bytes(c, op):
@@ -558,6 +561,7 @@ def precomp_leg(c, steps, warmup):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev.index) as clk:
+        torch.cuda.nvtx.range_push("precomp_timed")
         e0.record(stream)
         for _ in range(steps):
             ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
@@ -565,6 +569,7 @@ def precomp_leg(c, steps, warmup):
             evs.append(ev)
         e1.record(stream)
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
     launches = lib.so3g_launch_count() - n0
     ms = e0.elapsed_time(e1) / steps
     tm = float(np.mean([a.elapsed_time(b) for a, b, _, _ in evs]))
@@ -581,9 +586,11 @@ def precomp_leg(c, steps, warmup):
     return {"value": N / (ms * 1e-3), "ms_per_step": ms, "op_ms": {"to_map": tm, "from_map": fm},
             "pointing_matrix_ms": pm_ms,
             "roofline": {"bound": "hbm", "kernel": "precomp from_map", "achieved": ach_fm,
-                         "peak": hbm, "unit": "GB/s", "frac": ach_fm / hbm, "traffic": None,
+                         "peak": hbm, "unit": "GB/s", "frac": ach_fm / hbm,
+                         "traffic": MEASURED_TRAFFIC_PRECOMP["from_map"] * N,
                          "bytes_per_sample": b_fm, "peak_kind": kind,
                          "to_map": {"achieved": ach_tm, "frac": ach_tm / hbm,
+                                    "traffic": MEASURED_TRAFFIC_PRECOMP["to_map"] * N,
                                     "bytes_per_sample": b_tm}},
             "clocks": clk.summary(), "gpu_launches": int(launches)}
 
