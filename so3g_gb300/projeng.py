@@ -22,6 +22,8 @@ tensors too.  Every call runs the CUDA kernels: there is no CPU path.
 import ctypes
 import os
 
+import weakref
+
 import numpy as np
 import torch
 
@@ -677,6 +679,30 @@ def _as_int(x, what):
         raise TypeError("Failed to interpret argument \"%s\" as int." % what) from None
 
 
+# Detector tensors already found free of NaN: the check reads its result
+# on the host (a stream synchronisation), which iterative callers passing
+# the same tensor call after call need not repeat.  An entry holds while it
+# is the same tensor object, storage and version counter (any in-place
+# write bumps the version).
+_CHECKED = {}
+_CHECKED_MAX = 64
+
+
+def _nan_key(t):
+    return (t.data_ptr(), t._version, tuple(t.shape), tuple(t.stride()), str(t.device))
+
+
+def _nan_checked(t):
+    e = _CHECKED.get(id(t))
+    return e is not None and e[0]() is t and e[1] == _nan_key(t)
+
+
+def _remember_checked(t):
+    if len(_CHECKED) >= _CHECKED_MAX:
+        _CHECKED.clear()
+    _CHECKED[id(t)] = (weakref.ref(t), _nan_key(t))
+
+
 class ProjEngBase:
     """Common machinery of the ProjEng_* classes.  Subclasses fix the
     coordinate system, the pixelization, the tiling, the interpolation and
@@ -797,7 +823,12 @@ class ProjEngBase:
         bore = as_array(pbore, "boresight", "float64", (-1, 4))
         dets = as_array(pofs, "detectors", "float64", (-1, 4))
         if isinstance(dets, torch.Tensor):
-            bad = torch.nonzero(torch.isnan(dets).any(dim=1)).flatten().cpu().numpy()
+            if not _nan_checked(dets):
+                bad = torch.nonzero(torch.isnan(dets).any(dim=1)).flatten().cpu().numpy()
+                if not len(bad):
+                    _remember_checked(dets)
+            else:
+                bad = ()
         else:
             bad = np.nonzero(np.isnan(dets).any(axis=1))[0]
         if len(bad):

@@ -234,3 +234,38 @@ def test_host_signal_policy(monkeypatch):
     monkeypatch.setenv("SO3G_GB300_HOST_SIGNAL", "bogus")
     with pytest.raises(ValueError, match="SO3G_GB300_HOST_SIGNAL"):
         projeng.host_signal_policy()
+
+
+def test_detector_nan_check_remembers_clean_tensors():
+    """A detector tensor found free of NaN is not checked again while it is
+    the same tensor and unmodified; an in-place write brings the check
+    back."""
+    import torch
+    from so3g_gb300 import projeng
+    eng = so3g_gb300.ProjEng_CAR_TQU_NonTiled((10, 10, 1., 1., 5., 5.))
+    bore = torch.zeros((7, 4), dtype=torch.float64)
+    dets = torch.zeros((3, 4), dtype=torch.float64)
+    dets[:, 0] = 1.
+    eng._pointer(bore, dets)
+    assert projeng._nan_checked(dets)
+    eng._pointer(bore, dets)
+    dets[1, 2] = float("nan")
+    assert not projeng._nan_checked(dets)
+    with pytest.raises(ValueError, match="nan found at index 1"):
+        eng._pointer(bore, dets)
+    other = dets.clone()
+    assert not projeng._nan_checked(other)
+
+
+def test_device_ranges_to_host():
+    """DeviceRangesMatrix.to_host rebuilds the RangesMatrix from segments."""
+    import torch
+    from so3g_gb300.ranges import DeviceRangesMatrix
+    seg = torch.tensor([[0, 2, 5], [0, 7, 9], [2, 0, 10]], dtype=torch.int32)
+    d = DeviceRangesMatrix(seg, 3, 10, 10)
+    assert d.shape == (3, 10) and len(d) == 3 and d.n_seg == 3
+    m = d.mask()
+    want = np.zeros((3, 10), bool)
+    want[0, 2:5] = want[0, 7:9] = want[2, :] = True
+    assert np.array_equal(m, want)
+    assert np.array_equal(RangesMatrix.from_mask(want).mask(), want)
