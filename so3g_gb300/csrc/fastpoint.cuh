@@ -441,6 +441,40 @@ __device__ __forceinline__ bool fast_spin(int nc, float T, float Pr, const dfl &
     return true;
 }
 
+// Certified spin factors of a sample whose pixel is already certain (the
+// float32 tier of mixedpoint.cuh certified it): the double-float
+// quaternion and the spin quantities Nc, Ns, D formed by the same
+// operations as fast_native / fast_lon_spin (hence the same values), then
+// fast_spin.  False where that path would not apply or the float32
+// roundings are not certain.
+template <int C>
+__device__ __forceinline__ bool df_spin_only(const dfl (&qb)[4], const dfl (&qd)[4], int nc,
+                                             float T, float Pr, float *pf) {
+    if (nc == 1) {
+        pf[0] = T;
+        pf[1] = pf[2] = 0.f;
+        return true;
+    }
+    dfl a, b, c, d;
+    df_qmul(qb, qd, a, b, c, d);
+    dfl Nc, Ns, D;
+    if (C == SO3G_COORD_CAR) {
+        const dfl cos_t = df_dot<4>({a, b, c, d}, {a, df_neg(b), df_neg(c), d});
+        if (!(fabsf(cos_t.hi) < 0.998f)) return false;
+        const dfl cd = df_mul(c, d), ab = df_mul(a, b);
+        Nc = df_dot<2>({a, b}, {c, df_neg(d)});
+        Ns = df_add(cd, ab);
+        D = df_mulf(df_sub(dfl{1.f, 0.f}, df_mul(cos_t, cos_t)), 0.25f);
+    } else {
+        const dfl n = df_dot<2>({a, d}, {a, d});
+        if (!(n.hi > 1e-4f)) return false;
+        Nc = df_dot<2>({a, d}, {a, df_neg(d)});
+        Ns = df_mulf(df_mul(a, d), 2.f);
+        D = df_mul(n, n);
+    }
+    return fast_spin<true>(nc, T, Pr, Nc, Ns, D, pf);
+}
+
 // Integer part of a double-float whose fraction is certified to be at
 // least e from 0 and 1; false otherwise.
 __device__ __forceinline__ bool df_floor_cert(dfl x, float e, int &i) {

@@ -129,13 +129,56 @@ __device__ __forceinline__ bool df_gather(const GatherArgs &a, int det, int t, c
     return true;
 }
 
+// One sample of the certified float32 tier's fallback through the full
+// certified double-float pointing and certified float32 roundings of the
+// reference's float64 sums; false (signal untouched) when any of them is
+// not certain.
+template <int C, int P>
+__device__ __forceinline__ bool df_gather_cert(const GatherArgs &a, int det, int t,
+                                               const dfl (&qd)[4], float T, float Pr) {
+    constexpr int NT = PixTraits<P>::taps;
+    const double *bp = a.bore + 4LL * t;
+    const double2 lo = __ldg(reinterpret_cast<const double2 *>(bp));
+    const double2 hi = __ldg(reinterpret_cast<const double2 *>(bp) + 1);
+    dfl qb[4];
+    if (!(df_split(lo.x, qb[0]) & df_split(lo.y, qb[1]) & df_split(hi.x, qb[2]) &
+          df_split(hi.y, qb[3])))
+        return false;
+    int pix[NT][3];
+    float pf[3], w[NT];
+    int n = 0;
+    const int nc = a.g.ncomp;
+    if (!fast_pointing<C, P>(a.g, a.ft, a.fc, qb, qd, nc, T, Pr, pix, w, n, pf)) return false;
+    if (n == 0) return true;
+    float *sp = a.signal + det * a.sig_stride + t;
+    float s = *sp;
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < NT; k++) {
+        if (k >= n || !ok) break;
+        long long off, plane;
+        const int bad = locate<P>(a.g, pix[k], &off, &plane);
+        if (bad >= 0) {
+            record_missing_tile(a.err, bad);
+            continue;
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+            if (ok && c < nc) ok = fast_accum(s, __ldg(a.map + off + c * plane), pf[c], w[k]);
+    }
+    if (ok) *sp = s;
+    return ok;
+}
+
 // Compiled for 5 resident blocks per SM (at most 51 registers; mixed
 // pointing: 7), one variant per pointing mode (0 exact, 1 certified, 2
-// mixed).
+// mixed).  The certified and mixed variants of the nearest-neighbour
+// CAR/TAN/ZEA/SIN and HEALPix pixelizations take the float32 tier first.
 template <int C, int P, int MODE>
 __global__ void __launch_bounds__(kBlock, MODE == 2 ? 7 : 5) k_from_map(GatherArgs a) {
     constexpr bool kFastOK = FastEligible<C, P>::value && MODE >= 1;
-    constexpr bool kMixedOK = MixedEligible<C, P>::value && MODE == 2;
+    constexpr bool kMixedOK = MixedEligible<C, P>::value && MODE >= 1;
+    constexpr bool kCert = MODE == 1;
     __shared__ int s_queue[!kFastOK ? 1 : (kMixedOK ? 2 : 1) * (kBlock / 32) * kWarpQueue];
     __shared__ WarpPiece s_wp[kFastOK ? kBlock / 32 : 1];
     int det, t0, t1;
@@ -178,6 +221,64 @@ __global__ void __launch_bounds__(kBlock, MODE == 2 ? 7 : 5) k_from_map(GatherAr
     for (int r = 0; r < rounds; r++) {
         const int t = t0 + r * blockDim.x + threadIdx.x;
         bool push = false, push_df = false;
+        if (kMixedOK && mixed && kCert) {
+            if (t < t1) {
+                float *sp = a.signal + det * a.sig_stride + t;
+                const float s_in = *sp;
+                // The float32 tier's pixel from the float64 boresight's
+                // double-float split, the certified spin factors from the
+                // split itself, and certified float32 roundings of the
+                // reference's float64 sums.
+                const double *bp = a.bore + 4LL * t;
+                const double2 lo = __ldg(reinterpret_cast<const double2 *>(bp));
+                const double2 hi = __ldg(reinterpret_cast<const double2 *>(bp) + 1);
+                dfl qb[4];
+                bool ok = df_split(lo.x, qb[0]) & df_split(lo.y, qb[1]) &
+                          df_split(hi.x, qb[2]) & df_split(hi.y, qb[3]);
+                const float qbf[4] = {qb[0].hi, qb[1].hi, qb[2].hi, qb[3].hi};
+                int pix[3];
+                float pf[3];
+                bool on = false;
+                ok = ok && mixed_pointing<C, P, false>(a.g, a.ft, a.mc, qbf, qd32, nc, T, Pr,
+                                                       pix, on, pf);
+                if (ok && on) ok = df_spin_only<C>(qb, qd, nc, T, Pr, pf);
+                if (!ok) {
+                    push_df = true;
+                } else if (on) {
+                    long long off, plane;
+                    const int bad = locate<P>(a.g, pix, &off, &plane);
+                    if (bad >= 0) {
+                        record_missing_tile(a.err, bad);
+                    } else {
+                        // src/Projection.cxx:1763-1765, component by component.
+                        float s = s_in;
+#pragma unroll
+                        for (int c = 0; c < 3; c++)
+                            if (ok && c < nc)
+                                ok = fast_accum(s, __ldg(a.map + off + c * plane), pf[c]);
+                        if (ok) *sp = s;
+                        push = !ok;
+                    }
+                }
+            }
+            qn = warp_enqueue(wq, qn, push, t);
+            if (qn > kWarpQueue - 32) drain_exact();
+            qdf = warp_enqueue(wdf, qdf, push_df, t);
+            if (qdf >= 32 || (r == rounds - 1 && qdf > 0)) {
+                __syncwarp();
+                for (int base = 0; base < qdf; base += 32) {
+                    const int i = base + (threadIdx.x & 31);
+                    const int ts = i < qdf ? wdf[i] : 0;
+                    const bool px = i < qdf && !df_gather_cert<C, P>(a, det, ts, wp->qd, T, Pr);
+                    qn = warp_enqueue(wq, qn, px, ts);
+                    if (qn > kWarpQueue - 32) drain_exact();
+                }
+                __syncwarp();
+                qdf = 0;
+            }
+            if (qn > kWarpQueue - 32 || r == rounds - 1) drain_exact();
+            continue;
+        }
         if (kMixedOK && mixed) {
             if (t < t1) {
                 // The signal is loaded before the pointing is evaluated, so

@@ -280,7 +280,7 @@ __device__ __forceinline__ bool mixed_flat_pixel(const DGeom &g, const MixedCons
 
 // The float32 tier for CAR with a nearest-neighbour flat pixelizor.
 // Returns false when the sample must go to the double-float path.
-template <int P>
+template <int P, bool SPIN>
 __device__ __forceinline__ bool mixed_car(const DGeom &g, const FastTables &ft,
                                           const MixedConst &mc, const float (&qb)[4],
                                           const float (&qd)[4], int nc, float T, float Pr,
@@ -288,7 +288,7 @@ __device__ __forceinline__ bool mixed_car(const DGeom &g, const FastTables &ft,
     MixedLonLat o;
     if (!mixed_lonlat(ft, mc, qb, qd, o)) return false;
     if (!mixed_flat_pixel<P>(g, mc, o.lon, o.lat, o.elon, o.elat, pix, on)) return false;
-    if (on) mixed_spin(o, nc, T, Pr, pf);
+    if (SPIN && on) mixed_spin(o, nc, T, Pr, pf);
     return true;
 }
 
@@ -302,7 +302,7 @@ __device__ __forceinline__ bool mixed_car(const DGeom &g, const FastTables &ft,
 // +- 20u scales u, v and n; plus the float32 roundings.  False (double-
 // float path) far from the projection's pole: TAN with cos(theta) < 0.1,
 // ZEA and SIN with n < 0.25 (theta > 120 deg).
-template <int C, int P>
+template <int C, int P, bool SPIN>
 __device__ __forceinline__ bool mixed_zen(const DGeom &g, const MixedConst &mc,
                                           const float (&qb)[4], const float (&qd)[4], int nc,
                                           float T, float Pr, int *pix, bool &on, float *pf) {
@@ -339,7 +339,7 @@ __device__ __forceinline__ bool mixed_zen(const DGeom &g, const MixedConst &mc,
         e = fmaf(22.f * kU, r, 16.f * kU * (fabsf(X) + fabsf(Y)));
     }
     if (!mixed_flat_pixel<P>(g, mc, X, Y, e, e, pix, on)) return false;
-    if (!on) return true;
+    if (!on || !SPIN) return true;
     // Spin factors (:1180-1209) with c = (a^2 - d^2)/n, s = 2ad/n.
     if (nc == 1) {
         pf[0] = T;
@@ -367,7 +367,7 @@ __device__ __forceinline__ bool mixed_zen(const DGeom &g, const MixedConst &mc,
 // <= 2^-21.41 for |lat| <= pi), every integer decision certified against
 // the propagated error bound (x1.5 safety).  Returns false when the sample
 // must go to the double-float path; the pixel is always on the map.
-template <int P>
+template <int P, bool SPIN>
 __device__ __forceinline__ bool mixed_healpix(const DGeom &g, const FastTables &ft,
                                               const MixedConst &mc, const float (&qb)[4],
                                               const float (&qd)[4], int nc, float T, float Pr,
@@ -456,23 +456,25 @@ __device__ __forceinline__ bool mixed_healpix(const DGeom &g, const FastTables &
         pix[0] = (int)(ip / g.nppt);
         pix[1] = (int)(ip % g.nppt);
     }
-    mixed_spin(o, nc, T, Pr, pf);
+    if (SPIN) mixed_spin(o, nc, T, Pr, pf);
     return true;
 }
 
 // The float32 tier of one sample for pixelization P: one tap (weight 1)
-// when `on`.  False hands the sample to the double-float path.
-template <int C, int P>
+// when `on`.  False hands the sample to the double-float path.  SPIN =
+// false: the pixel only (the caller forms certified spin factors).
+template <int C, int P, bool SPIN = true>
 __device__ __forceinline__ bool mixed_pointing(const DGeom &g, const FastTables &ft,
                                                const MixedConst &mc, const float (&qb)[4],
                                                const float (&qd)[4], int nc, float T, float Pr,
                                                int *pix, bool &on, float *pf) {
     if (P == PX_HP_NT || P == PX_HP_T) {
         on = true;
-        return mixed_healpix<P>(g, ft, mc, qb, qd, nc, T, Pr, pix, pf);
+        return mixed_healpix<P, SPIN>(g, ft, mc, qb, qd, nc, T, Pr, pix, pf);
     }
-    if (C == SO3G_COORD_CAR) return mixed_car<P>(g, ft, mc, qb, qd, nc, T, Pr, pix, on, pf);
-    return mixed_zen<C, P>(g, mc, qb, qd, nc, T, Pr, pix, on, pf);
+    if (C == SO3G_COORD_CAR)
+        return mixed_car<P, SPIN>(g, ft, mc, qb, qd, nc, T, Pr, pix, on, pf);
+    return mixed_zen<C, P, SPIN>(g, mc, qb, qd, nc, T, Pr, pix, on, pf);
 }
 
 }  // namespace so3g

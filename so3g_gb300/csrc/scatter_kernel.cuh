@@ -129,11 +129,12 @@ __device__ __noinline__ void exact_sample(const ScatterArgs &a, int det, int t, 
     }
 }
 
-// One sample of the mixed-pointing fallback through the double-float
+// One sample of the float32 tier's fallback through the double-float
 // pointing, added with plain atomics; false (nothing added) when its pixel
-// is not certified.  Its spin factors, like the float32 tier's, are float32
-// evaluations (the mixed-precision contract).
-template <int C, int P, bool WEIGHT>
+// (CERT: or a spin factor) is not certified.  Without CERT its spin
+// factors, like the float32 tier's, are float32 evaluations (the
+// mixed-precision contract).
+template <int C, int P, bool WEIGHT, bool CERT = false>
 __device__ __forceinline__ bool df_sample(const ScatterArgs &a, int det, int t, const dfl (&qd)[4], float T,
                           float Pr, float det_wt, const int *mult, unsigned vmask) {
     constexpr int NT = PixTraits<P>::taps;
@@ -148,7 +149,7 @@ __device__ __forceinline__ bool df_sample(const ScatterArgs &a, int det, int t, 
     int pix[NT][3];
     float w[NT], pf[3];
     int n = 0;
-    if (!fast_pointing<C, P, false>(a.g, a.ft, a.fc, qb, qd, a.g.ncomp, T, Pr, pix, w, n, pf))
+    if (!fast_pointing<C, P, CERT>(a.g, a.ft, a.fc, qb, qd, a.g.ncomp, T, Pr, pix, w, n, pf))
         return false;
     const float sig = (!WEIGHT && n > 0) ? __ldg(a.signal + det * a.sig_stride + t) : 0.f;
     for (int k = 0; k < n; k++) {
@@ -172,7 +173,12 @@ __device__ __forceinline__ bool df_sample(const ScatterArgs &a, int det, int t, 
 template <int C, int P, int MODE>
 struct PointingVariant {
     static constexpr bool fast = FastEligible<C, P>::value && MODE >= 1;
-    static constexpr bool mixed = MixedEligible<C, P>::value && MODE == 2;
+    // The float32 tier decides the pixel (mixed pointing: and the spin
+    // factors); the samples it leaves go to the double-float path.
+    static constexpr bool mixed = MixedEligible<C, P>::value && MODE >= 1;
+    // Certified pointing: spin factors certified in double-float
+    // (df_spin_only) after the float32 tier's pixel.
+    static constexpr bool cert = MODE == 1;
 };
 
 // Shared ints of a block's fallback queues: per warp, one queue for the
@@ -256,10 +262,28 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
         if (live) {
             bool done = false;
             if (kMixedOK && mixed) {
-                float qb[4];
-                load_bore_f32(a.bore32, a.bore, t, qb);
-                bool on = false;
-                if (mixed_pointing<C, P>(a.g, a.ft, a.mc, qb, qd32, nc, T, Pr, pix[0], on, pf)) {
+                bool ok, on = false;
+                if constexpr (PointingVariant<C, P, MODE>::cert) {
+                    // The float32 tier's pixel from the float64 boresight's
+                    // double-float split (hi: within u(1 + 2^-22) of it),
+                    // the certified spin factors from the split itself.
+                    const double *bp = a.bore + 4LL * t;
+                    const double2 lo = __ldg(reinterpret_cast<const double2 *>(bp));
+                    const double2 hi = __ldg(reinterpret_cast<const double2 *>(bp) + 1);
+                    dfl qb[4];
+                    ok = df_split(lo.x, qb[0]) & df_split(lo.y, qb[1]) & df_split(hi.x, qb[2]) &
+                         df_split(hi.y, qb[3]);
+                    const float qbf[4] = {qb[0].hi, qb[1].hi, qb[2].hi, qb[3].hi};
+                    ok = ok && mixed_pointing<C, P, false>(a.g, a.ft, a.mc, qbf, qd32, nc, T, Pr,
+                                                           pix[0], on, pf);
+                    if (ok && on) ok = df_spin_only<C>(qb, qd, nc, T, Pr, pf);
+                } else {
+                    float qb[4];
+                    load_bore_f32(a.bore32, a.bore, t, qb);
+                    ok = mixed_pointing<C, P>(a.g, a.ft, a.mc, qb, qd32, nc, T, Pr, pix[0], on,
+                                              pf);
+                }
+                if (ok) {
                     n = on ? 1 : 0;
                     w[0] = 1.f;
                 } else {
@@ -325,8 +349,8 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
                 const int i = base + (threadIdx.x & 31);
                 const int ts = i < qdf ? wdf[i] : 0;
                 const bool px =
-                    i < qdf && !df_sample<C, P, WEIGHT>(a, det, ts, wp->qd, T, Pr, det_wt,
-                                                        mult, vmask);
+                    i < qdf && !df_sample<C, P, WEIGHT, PointingVariant<C, P, MODE>::cert>(
+                                   a, det, ts, wp->qd, T, Pr, det_wt, mult, vmask);
                 qn = warp_enqueue(wq, qn, px, ts);
                 if (qn > kWarpQueue - 32) drain_exact();
             }
