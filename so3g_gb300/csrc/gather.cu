@@ -31,8 +31,51 @@ struct GatherArgs {
     FastConst fc;
     MixedConst mc;
     const float4 *bore32;   // float32 boresight (mixed pointing), or NULL
-    const float4 *map32;    // float32 (T, Q, U, 0) per pixel (mixed, untiled), or NULL
+    const float4 *map32;    // float32 (T, Q, U, 0) per pixel (mixed pointing), or NULL
 };
+
+// Largest parent map (pixels) that gets the float32 copy when tiled: the
+// copy spans the parent map (16 bytes per pixel), present tiles or not.
+constexpr long long kMap32TiledMaxPixels = 1LL << 28;
+
+// Index of a located sample's pixel in the float32 map copy: its element
+// offset for an untiled map; for a tiled map its pixel in the parent map
+// (flat: row-major over (ny, nx); HEALPix: the NEST index tile * nppt + sub).
+template <int P>
+__device__ __forceinline__ long long map32_index(const DGeom &g, const int *pix, long long off) {
+    if (P == PX_FLAT_T_NN || P == PX_FLAT_T_BL) {
+        const int t = pix[0], row = t / g.ntx, col = t - row * g.ntx;
+        return (long long)(row * g.ty + pix[1]) * g.nx + (long long)col * g.tx + pix[2];
+    }
+    if (P == PX_HP_T) return (long long)pix[0] * g.nppt + pix[1];
+    return off;
+}
+
+// The float32 copy of a tiled map over its parent map's pixels (absent
+// tiles: zeros, never read -- their samples raise the missing-tile error).
+template <int P>
+__global__ void k_map_f32_tiled(DGeom g, const double *map, long long npix, float4 *out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npix) return;
+    int pix[3];
+    if (P == PX_HP_T) {
+        pix[0] = (int)(i / g.nppt);
+        pix[1] = (int)(i - (long long)pix[0] * g.nppt);
+        pix[2] = 0;
+    } else {
+        const int gy = (int)(i / g.nx), gx = (int)(i - (long long)gy * g.nx);
+        const int row = gy / g.ty, col = gx / g.tx;
+        pix[0] = row * g.ntx + col;
+        pix[1] = gy - row * g.ty;
+        pix[2] = gx - col * g.tx;
+    }
+    float v[3] = {0.f, 0.f, 0.f};
+    long long off, plane;
+    if (locate<P>(g, pix, &off, &plane) < 0)
+        for (int c = 0; c < g.ncomp && c < 3; c++)
+            v[c] = __double2float_rn(__ldg(map + off + c * plane));
+    out[i] = make_float4(v[0], v[1], v[2], 0.f);
+}
 
 // The untiled map's components as float32, pixel by pixel (one 16-byte
 // load per sample in the mixed from_map).
@@ -115,7 +158,7 @@ __device__ __forceinline__ bool df_gather(const GatherArgs &a, int det, int t, c
             continue;
         }
         if (a.map32) {
-            const float4 m = __ldg(a.map32 + off);
+            const float4 m = __ldg(a.map32 + map32_index<P>(a.g, pix[k], off));
             s = fmaf(m.x, pf[0] * w[k], s);
             if (nc > 1) s = fmaf(m.y, pf[1] * w[k], s);
             if (nc > 2) s = fmaf(m.z, pf[2] * w[k], s);
@@ -301,7 +344,7 @@ __global__ void __launch_bounds__(kBlock, MODE == 2 ? 7 : 5) k_from_map(GatherAr
                             // float32 terms (the mixed-precision contract).
                             float s = s_in;
                             if (a.map32) {
-                                const float4 m = __ldg(a.map32 + off);
+                                const float4 m = __ldg(a.map32 + map32_index<P>(a.g, pix, off));
                                 s = fmaf(m.x, pf[0], s);
                                 if (nc > 1) s = fmaf(m.y, pf[1], s);
                                 if (nc > 2) s = fmaf(m.z, pf[2], s);
@@ -430,17 +473,25 @@ extern "C" int so3g_proj_from_map(const so3g_pixelization *pz, const double *bor
     L.grid = dim3((unsigned)n_det, (unsigned)((n_time + L.a.piece - 1) / L.a.piece));
     L.stream = (cudaStream_t)stream;
     L.a.bore32 = bore_f32(pz, L.a.fast, boresight, n_time, L.stream);
-    // Mixed pointing on an untiled map: a float32 copy of the map, read with
-    // one 16-byte load per sample.
+    // Mixed pointing: a float32 copy of the map, pixel by pixel (over the
+    // parent map when tiled), read with one 16-byte load per sample.
     float4 *map32 = nullptr;
-    if (L.a.bore32 && !pz->tiled) {
-        const long long npix = pz->pix_sys == SO3G_PIX_HEALPIX
-                                   ? L.a.g.npix
-                                   : (long long)L.a.g.ny * L.a.g.nx;
+    const long long npix = pz->pix_sys == SO3G_PIX_HEALPIX ? L.a.g.npix
+                                                           : (long long)L.a.g.ny * L.a.g.nx;
+    const int kind = pix_kind(pz);
+    const bool tiled_ok = kind == PX_FLAT_T_NN || kind == PX_HP_T;
+    if (L.a.bore32 && (!pz->tiled || (tiled_ok && npix <= kMap32TiledMaxPixels))) {
         if (cudaMallocAsync(reinterpret_cast<void **>(&map32), sizeof(float4) * (size_t)npix,
                             L.stream) == cudaSuccess) {
-            k_map_f32<<<(unsigned)((npix + kBlock - 1) / kBlock), kBlock, 0, L.stream>>>(
-                map->data, pz->n_comp, npix, map32);
+            const unsigned blocks = (unsigned)((npix + kBlock - 1) / kBlock);
+            if (!pz->tiled)
+                k_map_f32<<<blocks, kBlock, 0, L.stream>>>(map->data, pz->n_comp, npix, map32);
+            else if (kind == PX_HP_T)
+                k_map_f32_tiled<PX_HP_T><<<blocks, kBlock, 0, L.stream>>>(L.a.g, map->data,
+                                                                          npix, map32);
+            else
+                k_map_f32_tiled<PX_FLAT_T_NN><<<blocks, kBlock, 0, L.stream>>>(
+                    L.a.g, map->data, npix, map32);
             if (after_launch("map float32 copy") != SO3G_OK) {
                 cudaFreeAsync(map32, L.stream);
                 map32 = nullptr;
