@@ -2,11 +2,15 @@
 // accumulated into the float32 signal exactly as the reference does (each
 // term added in float64 and rounded to float32).
 //
-// CAR, TAN, ZEA and SIN with flat pixelizors use the certified double-float
-// pointing of fastpoint.cuh (when GatherArgs::fast is set);
-// samples it cannot certify are queued in shared memory (per warp) and
-// finished by the exact float64 pointing, so every sample's result equals
-// the exact path's.
+// CAR, TAN, ZEA and SIN with flat pixelizors and CAR HEALPix use the
+// certified double-float pointing of fastpoint.cuh (when GatherArgs::fast
+// is set), their nearest-neighbour forms behind the float32 tier of
+// mixedpoint.cuh (certified mode: the pixel from it, spin factors and
+// terms certified in double-float; mixed mode: float32 spin factors and
+// terms).  Samples a tier cannot certify are queued in shared memory (per
+// warp) and go, 32 at a time, to the double-float and then the exact
+// float64 pointing; in certified mode every sample's result equals the
+// exact path's.
 
 #include "host.h"
 

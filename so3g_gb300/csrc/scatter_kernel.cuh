@@ -9,11 +9,14 @@
 // (compensated float32) and flushed with one float64 atomic per run and
 // component.  The ATOMIC accumulator adds every term on its own.
 //
-// Pointing: CAR, TAN, ZEA and SIN with flat pixelizors use the certified
-// double-float pointing of fastpoint.cuh when ScatterArgs::fast is set;
-// samples it cannot certify are queued in shared memory (per warp) and
-// recomputed by the exact float64 pointing, with plain atomics, when the
-// queue fills and at the end of the piece.  Every other case uses the exact pointing.
+// Pointing (ScatterArgs::fast): CAR, TAN, ZEA and SIN with flat pixelizors
+// and CAR HEALPix use the certified double-float pointing of fastpoint.cuh.
+// Their nearest-neighbour forms take the float32 tier of mixedpoint.cuh
+// first: the mixed mode for the pixel and the spin factors, the certified
+// mode for the pixel only (its spin factors from df_spin_only).  Samples a
+// tier cannot certify are queued in shared memory (per warp) and go, 32 at
+// a time, to the double-float path and from there to the exact float64
+// pointing, with plain atomics.  Every other case uses the exact pointing.
 #pragma once
 
 #include "host.h"
