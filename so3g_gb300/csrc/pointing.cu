@@ -231,6 +231,45 @@ __global__ void k_pixels_fix(int *pixel, int n_det, int n_time, int sub) {
     }
 }
 
+// ---- taps of one sample --------------------------------------------------------
+
+// The GetPixels taps of one sample (Pixelizor*::GetPixels): the certified
+// double-float pointing where it applies and decides -- its pixel
+// decisions are the exact path's; no spin factors are formed -- else the
+// exact float64 path.  qd: the detector's double-float split (a.fast).
+template <int C, int P>
+__device__ __forceinline__ int sample_taps(const PointArgs &a, const QuatD &ofs,
+                                           const dfl (&qd)[4], int t, int (*pix)[3], float *w) {
+    if constexpr (FastEligible<C, P>::value) {
+        if (a.fast) {
+            const double2 lo = __ldg(reinterpret_cast<const double2 *>(a.bore + 4LL * t));
+            const double2 hi = __ldg(reinterpret_cast<const double2 *>(a.bore + 4LL * t) + 1);
+            dfl qb[4];
+            const bool ok = df_split(lo.x, qb[0]) & df_split(lo.y, qb[1]) &
+                            df_split(hi.x, qb[2]) & df_split(hi.y, qb[3]);
+            int n = 0;
+            float pf[3];
+            if (ok && fast_pointing<C, P, false>(a.g, a.ft, a.fc, qb, qd, 1, 1.f, 0.f, pix, w, n,
+                                                 pf))
+                return n;
+        }
+    }
+    double c[4];
+    get_coords<C>(a.g.lut, load_quat(a.bore + 4LL * t), ofs, c);
+    return get_pixels<P>(a.g, c, pix, w);
+}
+
+// The detector's double-float split, where the certified pointing is used.
+template <int C, int P>
+__device__ __forceinline__ void det_split(const PointArgs &a, const QuatD &ofs, dfl (&qd)[4]) {
+    if (FastEligible<C, P>::value && a.fast) {
+        qd[0] = df_of(ofs.a);
+        qd[1] = df_of(ofs.b);
+        qd[2] = df_of(ofs.c);
+        qd[3] = df_of(ofs.d);
+    }
+}
+
 // ---- tile_hits ------------------------------------------------------------
 
 template <int C, int P>
@@ -241,16 +280,14 @@ __global__ void __launch_bounds__(kBlock) k_tile_hits(PointArgs a) {
     const long long p0 = (long long)blockIdx.y * a.piece;
     const int t1 = (int)min((long long)a.n_time, p0 + a.piece);
     const QuatD ofs = load_quat(a.dets + 4LL * det);
+    dfl qd[4];
+    det_split<C, P>(a, ofs, qd);
     for (int base = (int)p0 + (threadIdx.x & ~31); base < t1; base += blockDim.x) {
         const int t = base + lane;
         int pix[NT][3];
         float w[NT];
         int n = 0;
-        if (t < t1) {
-            double c[4];
-            get_coords<C>(a.g.lut, load_quat(a.bore + 4LL * t), ofs, c);
-            n = get_pixels<P>(a.g, c, pix, w);
-        }
+        if (t < t1) n = sample_taps<C, P>(a, ofs, qd, t, pix, w);
 #pragma unroll
         for (int k = 0; k < NT; k++) {
             int key = (k < n && pix[k][0] >= 0 && pix[k][0] < a.n_tile) ? pix[k][0] : -1;
@@ -268,14 +305,13 @@ __global__ void __launch_bounds__(kBlock) k_tile_hits(PointArgs a) {
 // ---- domain edges -----------------------------------------------------------
 
 template <int C, int P>
-__device__ __forceinline__ int sample_domain(const PointArgs &a, const QuatD &ofs, int t) {
+__device__ __forceinline__ int sample_domain(const PointArgs &a, const QuatD &ofs,
+                                             const dfl (&qd)[4], int t) {
     // pixel_ranges :1489-1506, tile_ranges :1655-1670
     constexpr int NT = PixTraits<P>::taps;
-    double c[4];
     int pix[NT][3];
     float w[NT];
-    get_coords<C>(a.g.lut, load_quat(a.bore + 4LL * t), ofs, c);
-    int n = get_pixels<P>(a.g, c, pix, w);
+    int n = sample_taps<C, P>(a, ofs, qd, t, pix, w);
     long long samp = -1;
 #pragma unroll
     for (int k = 0; k < NT; k++) {
@@ -313,11 +349,13 @@ __global__ void __launch_bounds__(kBlock) k_domain_edges(PointArgs a) {
     const long long p0 = (long long)blockIdx.y * a.piece;
     const int t1 = (int)min((long long)a.n_time, p0 + a.piece);
     const QuatD ofs = load_quat(a.dets + 4LL * det);
+    dfl qd[4];
+    det_split<C, P>(a, ofs, qd);
     const int nwarp = blockDim.x >> 5;
     for (long long s = p0 + (long long)warp * 31; s < t1; s += (long long)nwarp * 31) {
         const long long t = s - 1 + lane;
         int lab = INT_MIN;  // "before the first sample"
-        if (t >= 0 && t < t1) lab = sample_domain<C, P>(a, ofs, (int)t);
+        if (t >= 0 && t < t1) lab = sample_domain<C, P>(a, ofs, qd, (int)t);
         const int prev = __shfl_up_sync(kFull, lab, 1);
         const bool edge = lane > 0 && t < t1 && (t == 0 || lab != prev);
         if (edge) {

@@ -20,6 +20,7 @@ current stream (no copies); outputs created by the call are then CUDA
 tensors too.  Every call runs the CUDA kernels: there is no CPU path.
 """
 import ctypes
+import gc
 import os
 
 import weakref
@@ -1093,11 +1094,30 @@ def _edges_to_ranges(e, n_det, n_time, n_domain):
         ends = np.full(len(e), n_time, dtype=np.int64)
         same = e[1:, 0] == e[:-1, 0]
         ends[:-1][same] = e[1:, 1][same]
-        for (det, t, lab), end in zip(e.tolist(), ends.tolist()):
-            if lab < 0:
-                continue
-            target = par[lab] if lab < n_domain else ser[0]
-            target[det].append_interval_no_check(t, end)
+        keep = e[:, 2] >= 0
+        det, t, lab, ends = e[keep, 0], e[keep, 1], e[keep, 2], ends[keep]
+        # Domain index n_domain: the serial (shared) ranges.
+        tgt = np.minimum(lab, n_domain).astype(np.int64)
+        # Group by (domain, detector); within a group the intervals stay in
+        # time order (the stable sort keeps the (det, t) order).
+        key = tgt * n_det + det
+        g = np.argsort(key, kind="stable")
+        key, pairs = key[g], np.stack([t[g].astype(np.int64), ends[g]], axis=1)
+        cut = np.flatnonzero(np.diff(key)) + 1
+        starts = np.concatenate([[0], cut])
+        stops = np.concatenate([cut, [len(key)]])
+        # Millions of small interval lists: the cyclic garbage collector
+        # would rescan the growing heap many times over while they are made.
+        was_enabled = gc.isenabled()
+        gc.disable()
+        try:
+            for a, b in zip(starts.tolist(), stops.tolist()):
+                d, k = divmod(int(key[a]), n_det)
+                target = par[d] if d < n_domain else ser[0]
+                target[k]._segs = pairs[a:b].tolist()
+        finally:
+            if was_enabled:
+                gc.enable()
     return [par, ser]
 
 

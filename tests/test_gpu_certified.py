@@ -487,3 +487,36 @@ def test_certified_healpix_pointing_matrix(nest, tiled):
         out[mode] = [_np(x) for x in (pm_pix, pm_proj)]
     for a, b in zip(out[_abi.POINTING_EXACT], out[_abi.POINTING_CERTIFIED]):
         assert bits_equal(a, b)
+
+
+def _ranges_lists(R):
+    """pixel_ranges / tile_ranges output as nested lists of interval arrays."""
+    if hasattr(R, "ranges") and callable(getattr(R, "ranges")):
+        return np.asarray(R.ranges()).tolist()
+    if isinstance(R, (list, tuple)) or hasattr(R, "__iter__"):
+        return [_ranges_lists(x) for x in R]
+    return R
+
+
+@pytest.mark.parametrize("proj", ["CAR", "TAN"])
+@pytest.mark.parametrize("interpol", [None, "bilinear"])
+def test_certified_tile_hits_and_ranges(orc, proj, interpol):
+    """tile_hits, pixel_ranges and tile_ranges take the certified taps:
+    identical to the exact path on pixel-edge inputs."""
+    import torch
+    p, eng = _engine((300, 400), 0.5 * ARCMIN, True, proj=proj, interpol=interpol)
+    q = _edge_quats(orc, eng, proj, 30000, 23)
+    dets = np.array([[1., 0., 0., 0.], [np.cos(0.3), 0., 0., np.sin(0.3)]])
+    qd, dd = (torch.from_numpy(x).cuda() for x in (q, dets))
+    out = {}
+    for mode in (_abi.POINTING_EXACT, _abi.POINTING_CERTIFIED):
+        eng.pointing = mode
+        hits = np.asarray(eng.tile_hits(qd, dd))
+        pr = _ranges_lists(eng.pixel_ranges(qd, dd, None, 4))
+        groups = [[i for i in range(len(hits)) if hits[i] and i % 3 == g] for g in range(3)]
+        tr = _ranges_lists(eng.tile_ranges(qd, dd, groups))
+        out[mode] = (hits, pr, tr)
+    ex, ce = out[_abi.POINTING_EXACT], out[_abi.POINTING_CERTIFIED]
+    assert np.array_equal(ex[0], ce[0]) and ex[0].sum() > 0
+    assert ex[1] == ce[1]
+    assert ex[2] == ce[2]
