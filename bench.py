@@ -231,6 +231,12 @@ class ClockSampler:
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # nvidia-smi's start-up (NVML initialisation) can hold the GPU's
+            # work queue for ~100 ms: the timed region starts after its first
+            # reading, not during its start-up.
+            deadline = time.time() + 5.
+            while not self.lines and time.time() < deadline and self.proc.poll() is None:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
         return self
