@@ -286,6 +286,11 @@ MEASURED_TRAFFIC_PER_SAMPLE = {
     "mixed": {"to_map": (883.75e6 + 110.41e6) / 2e8,
               "from_map": (859.73e6 + 844.40e6) / 2e8},
 }
+# Float64-pipe lane operations per sample of the float64 path's to_map
+# (ncu sm__inst_executed_pipe_fp64.sum x 32 / samples, 200 detectors x 1M)
+# and the float64 FMA rate measured on a GB300 (1.6 lane-ops/clock/SM).
+FP64_OPS_PER_SAMPLE_TO_MAP = 1.018354e9 * 32 / 2e8
+FP64_LANE_OPS_PER_S = 5.0e11
 # The same for the Precomp kernels (ncu, 100 detectors x 1M samples).
 MEASURED_TRAFFIC_PRECOMP = {"to_map": (2.400763e9 + 3.709e6) / 1e8,
                             "from_map": (2.406085e9 + 413.98e6) / 1e8}
@@ -911,6 +916,15 @@ def main():
         f = res["fp64_path"]
         line["fp64_path"] = {"value": N / (f["ms_per_step"] * 1e-3), "op_ms": f["op_ms"],
                              "mixed_over_fp64": f["ms_per_step"] / ms}
+        if "to_map" in f["op_ms"]:
+            # Its bound: the float64 pipe (ncu: 163 float64-pipe lane
+            # operations per sample in to_map; the float64 FMA rate measured
+            # on a GB300: 5.0e11 lane-ops/s).
+            ach = FP64_OPS_PER_SAMPLE_TO_MAP * N / (f["op_ms"]["to_map"] * 1e-3)
+            line["fp64_path"]["roofline"] = {
+                "bound": "fp64 pipe", "kernel": "to_map", "achieved": ach,
+                "peak": FP64_LANE_OPS_PER_S, "unit": "lane-ops/s",
+                "frac": ach / FP64_LANE_OPS_PER_S}
     if "to_weight_map_ms" in res:
         line["to_weight_map"] = {"ms": res["to_weight_map_ms"],
                                  "samples_per_s": N / (res["to_weight_map_ms"] * 1e-3)}
