@@ -209,16 +209,23 @@ def _solve_lonlat(orc, eng, x_t, y_t, lon0, lat0, gam):
         return c[:, 0] / dx + crx - 1 + 0.5, c[:, 1] / dy + cry - 1 + 0.5
 
     for _ in range(6):
-        x, y = pixel_xy(lon, lat)
-        xa, ya = pixel_xy(lon + h, lat)
-        xb, yb = pixel_xy(lon, lat + h)
-        j11, j21 = (xa - x) / h, (ya - y) / h
-        j12, j22 = (xb - x) / h, (yb - y) / h
-        det = j11 * j22 - j12 * j21
-        ex, ey = x_t - x, y_t - y
-        lon = lon + (j22 * ex - j12 * ey) / det
-        lat = lat + (-j21 * ex + j11 * ey) / det
+        # Points at the projection's pole have a singular Jacobian: their
+        # NaN coordinates make samples that fall off the map.
+        with np.errstate(invalid="ignore", divide="ignore"):
+            lon, lat = _newton_step(pixel_xy, lon, lat, x_t, y_t, h)
     return lon, lat
+
+
+def _newton_step(pixel_xy, lon, lat, x_t, y_t, h):
+    """One Newton step towards pixel coordinates (x_t, y_t)."""
+    x, y = pixel_xy(lon, lat)
+    xa, ya = pixel_xy(lon + h, lat)
+    xb, yb = pixel_xy(lon, lat + h)
+    j11, j21 = (xa - x) / h, (ya - y) / h
+    j12, j22 = (xb - x) / h, (yb - y) / h
+    det = j11 * j22 - j12 * j21
+    ex, ey = x_t - x, y_t - y
+    return lon + (j22 * ex - j12 * ey) / det, lat + (-j21 * ex + j11 * ey) / det
 
 
 @pytest.mark.parametrize("proj", ["TAN", "ZEA", "SIN"])

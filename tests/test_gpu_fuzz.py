@@ -69,3 +69,29 @@ def test_random_geometry(gpulib, seed):
     assert bits_equal(ex[0], mx[0])
     for a, b in zip(ex[1:], mx[1:]):
         assert np.abs(a - b).max() <= 2e-5
+
+
+@pytest.mark.parametrize("seed", range(0, 30, 3))
+def test_random_geometry_to_map(gpulib, seed):
+    """to_map over the same random geometries: certified maps equal the
+    float64 path's up to float64 summation order, mixed ones within 1e-6
+    of the scale."""
+    import torch
+    kind, eng, maps, q, dets, resp = _case(seed)
+    rng = np.random.default_rng(seed)
+    sig = torch.from_numpy(rng.standard_normal((len(dets), len(q)), dtype=np.float32)).cuda()
+    qd, dd, rd = (torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in (q, dets, resp))
+
+    def flat(m):
+        if isinstance(m, list):
+            return np.concatenate([t.cpu().numpy().ravel() for t in m if t is not None])
+        return m.cpu().numpy().ravel()
+    out = {}
+    for mode in MODES:
+        eng.pointing = mode
+        out[mode] = flat(eng.to_map(None, qd, dd, rd, sig, None, None))
+    ex = out[_abi.POINTING_EXACT]
+    scale = np.abs(ex).max()
+    assert scale > 0
+    assert np.abs(out[_abi.POINTING_CERTIFIED] - ex).max() <= 1e-12 * scale
+    assert np.abs(out[_abi.POINTING_MIXED] - ex).max() <= 1e-6 * scale
