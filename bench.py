@@ -859,10 +859,11 @@ def main():
     cfg = {"workload": workload, "n_det": c["n_det"], "n_time": c["n_time"],
            "map": map_shape, "step": step_name,
            "l2": "inputs larger than L2 (TOD %.1f GB)" % (c["n_det"] * c["n_time"] * 4 / 1e9),
-           "precision": PRECISION[args.pointing] + (
-               "" if c["kind"] in ("car", "hp") or args.pointing != "mixed" else
-               " (mixed applies to CAR/TAN/ZEA/SIN nearest neighbour and HEALPix; this "
-               "pixelization runs certified)"),
+           "precision": (PRECISION[args.pointing] if c["kind"] in ("car", "hp") or
+                         args.pointing != "mixed" else
+                         "double-float pointing with the reference's bilinear taps (certified, "
+                         "float64 fallback), float32 spin factors, weights and products, "
+                         "float64 map accumulation"),
            "pointing": args.pointing,
            "parallelism": "replicas" if world > 1 else "single GPU"}
 

@@ -99,12 +99,14 @@ enum so3g_pointing {
      * exact path. */
     SO3G_POINTING_CERTIFIED = 1,
     /* Mixed precision (CAR, TAN, ZEA and SIN with nearest-neighbour flat
-     * pixelizors, and HEALPix; other pixelizations as
-     * SO3G_POINTING_CERTIFIED): float32 pointing whose
+     * pixelizors, and HEALPix): float32 pointing whose
      * pixel indices are certified equal to the exact ones (samples that
      * cannot be certified take the double-float, then the exact path).
-     * Spin factors and from_map terms are float32 evaluations: maps and
-     * signals agree with the exact path to ~1e-7 of their scale. */
+     * With bilinear flat pixelizors: the double-float pointing with the
+     * reference's taps.  Spin factors, interpolation weights and from_map
+     * terms are float32 evaluations: maps and signals agree with the exact
+     * path to ~1e-7 of their scale.  Other pixelizations as
+     * SO3G_POINTING_CERTIFIED. */
     SO3G_POINTING_MIXED = 2
 };
 

@@ -222,7 +222,8 @@ __device__ __forceinline__ bool df_gather_cert(const GatherArgs &a, int det, int
 // mixed).  The certified and mixed variants of the nearest-neighbour
 // CAR/TAN/ZEA/SIN and HEALPix pixelizations take the float32 tier first.
 template <int C, int P, int MODE>
-__global__ void __launch_bounds__(kBlock, MODE == 2 ? 7 : 5) k_from_map(GatherArgs a) {
+__global__ void __launch_bounds__(kBlock, MixedEligible<C, P>::value && MODE == 2 ? 7 : 5)
+    k_from_map(GatherArgs a) {
     constexpr bool kFastOK = FastEligible<C, P>::value && MODE >= 1;
     constexpr bool kMixedOK = MixedEligible<C, P>::value && MODE >= 1;
     constexpr bool kCert = MODE == 1;
@@ -268,6 +269,16 @@ __global__ void __launch_bounds__(kBlock, MODE == 2 ? 7 : 5) k_from_map(GatherAr
     for (int r = 0; r < rounds; r++) {
         const int t = t0 + r * blockDim.x + threadIdx.x;
         bool push = false, push_df = false;
+        if constexpr (MODE == 2 && !kMixedOK) {
+            // Mixed pointing where the float32 tier does not apply
+            // (bilinear): the double-float pointing with certified taps,
+            // float32 spin factors, weights and terms (df_gather); the exact
+            // path for the samples it leaves.
+            if (t < t1) push = !df_gather<C, P>(a, det, t, qd, T, Pr);
+            qn = warp_enqueue(wq, qn, push, t);
+            if (qn > kWarpQueue - 32 || r == rounds - 1) drain_exact();
+            continue;
+        }
         if (kMixedOK && mixed && kCert) {
             if (t < t1) {
                 float *sp = a.signal + det * a.sig_stride + t;
@@ -484,7 +495,10 @@ extern "C" int so3g_proj_from_map(const so3g_pixelization *pz, const double *bor
                                                            : (long long)L.a.g.ny * L.a.g.nx;
     const int kind = pix_kind(pz);
     const bool tiled_ok = kind == PX_FLAT_T_NN || kind == PX_HP_T;
-    if (L.a.bore32 && (!pz->tiled || (tiled_ok && npix <= kMap32TiledMaxPixels))) {
+    const bool mixed_bl = L.a.fast == SO3G_POINTING_MIXED && !pz->tiled &&
+                          pz->pix_sys == SO3G_PIX_FLAT && pz->interp == SO3G_INTERP_BILINEAR;
+    if ((L.a.bore32 || mixed_bl) &&
+        (!pz->tiled || (tiled_ok && npix <= kMap32TiledMaxPixels))) {
         if (cudaMallocAsync(reinterpret_cast<void **>(&map32), sizeof(float4) * (size_t)npix,
                             L.stream) == cudaSuccess) {
             const unsigned blocks = (unsigned)((npix + kBlock - 1) / kBlock);

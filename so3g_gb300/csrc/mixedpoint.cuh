@@ -58,12 +58,13 @@ struct MixedConst {
 };
 
 // Calls f.template go<MODE>() for the kernel variant of pointing mode `fast`.
+// Mixed pointing where the float32 tier does not apply (bilinear
+// pixelizors) runs the double-float tier with float32 spin factors and
+// terms.
 template <int C, int P, class F>
 int by_mode(int fast, F &f) {
-    if constexpr (MixedEligible<C, P>::value) {
-        if (fast == SO3G_POINTING_MIXED) return f.template go<2>();
-    }
     if constexpr (FastEligible<C, P>::value) {
+        if (fast == SO3G_POINTING_MIXED) return f.template go<2>();
         if (fast != SO3G_POINTING_EXACT) return f.template go<1>();
     }
     return f.template go<0>();

@@ -301,8 +301,9 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
                 dfl qb[4];
                 bool ok = df_split(lo.x, qb[0]) & df_split(lo.y, qb[1]) &
                           df_split(hi.x, qb[2]) & df_split(hi.y, qb[3]);
-                if (!(ok && fast_pointing<C, P>(a.g, a.ft, a.fc, qb, qd, nc, T, Pr, pix, w, n,
-                                                pf))) {
+                // Mixed pointing (bilinear): spin factors the nearest floats.
+                if (!(ok && fast_pointing<C, P, MODE != 2>(a.g, a.ft, a.fc, qb, qd, nc, T, Pr,
+                                                           pix, w, n, pf))) {
                     push = true;
                     n = 0;
                 }
@@ -365,7 +366,9 @@ __device__ __forceinline__ void scatter_piece(const ScatterArgs &a, int det, int
 }
 
 template <int C, int P, bool WEIGHT, int MODE>
-__global__ void __launch_bounds__(kBlock, MODE == 2 ? kMixedBlocksPerSM : kScatterBlocksPerSM)
+__global__ void __launch_bounds__(kBlock, PointingVariant<C, P, MODE>::mixed && MODE == 2
+                                              ? kMixedBlocksPerSM
+                                              : kScatterBlocksPerSM)
     k_scatter(ScatterArgs a) {
     __shared__ int s_queue[QueueInts<C, P, MODE>::value];
     __shared__ WarpPiece s_wp[kBlock / 32];
