@@ -82,3 +82,36 @@ def test_struct_layout_matches_header(tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(py), cname
         for f, _ in py._fields_:
             assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
+
+
+def test_new_entry_points_validate_arguments(lib):
+    """so3g_boresight, so3g_quat_left_multiply and the mask-segment entry
+    points reject bad arguments before any device work (no GPU needed)."""
+    import ctypes
+    import numpy as np
+    from so3g_gb300 import _abi
+    sl = _abi.SightLine()
+    sl.kind = 7
+    assert lib.so3g_boresight(ctypes.byref(sl), None, None, None, None, 10, None, None) == -1
+    assert "sight-line kind" in _abi.last_error()
+    sl.kind = _abi.SIGHT_NAIVE_AZEL
+    buf = np.zeros(64)
+    p = buf.ctypes.data
+    # naive az/el needs the times
+    assert lib.so3g_boresight(ctypes.byref(sl), None, p, p, None, 4, p, None) == -1
+    assert "NULL" in _abi.last_error()
+    assert lib.so3g_boresight(ctypes.byref(sl), p, p, p, None, -1, p, None) == -1
+    assert lib.so3g_boresight(ctypes.byref(sl), None, None, None, None, 0, None, None) == 0
+    # output not 16-byte aligned
+    assert lib.so3g_boresight(ctypes.byref(sl), p, p, p, None, 4, p + 8, None) == -1
+    assert "aligned" in _abi.last_error()
+    assert lib.so3g_quat_left_multiply(p, p, 4, p + 8, None) == -1
+    assert lib.so3g_quat_left_multiply(None, p, 4, p, None) == -1
+    assert lib.so3g_quat_left_multiply(p, p, 0, p, None) == 0
+    cnt = np.zeros(4, np.int32)
+    assert lib.so3g_mask_count_segments(p, -1, 10, 10, cnt.ctypes.data, None) == -1
+    assert lib.so3g_mask_count_segments(p, 4, 10, 5, cnt.ctypes.data, None) == -1
+    assert "det_stride" in _abi.last_error()
+    assert lib.so3g_mask_count_segments(p, 0, 10, 10, cnt.ctypes.data, None) == 0
+    assert lib.so3g_mask_fill_segments(p, 4, 10, 10, None, None, None, None, None) == -1
+    assert lib.so3g_mask_fill_segments(p, 4, 0, 10, None, None, None, None, None) == 0
