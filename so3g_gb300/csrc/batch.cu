@@ -14,7 +14,9 @@ namespace so3g {
 namespace {
 
 template <int C, int P, bool WEIGHT, int MODE>
-__global__ void __launch_bounds__(kBlock, MODE == 2 ? kMixedBlocksPerSM : kScatterBlocksPerSM)
+__global__ void __launch_bounds__(kBlock, PointingVariant<C, P, MODE>::mixed && MODE == 2
+                                              ? kMixedBlocksPerSM
+                                              : kScatterBlocksPerSM)
     k_scatter_batch(ScatterArgs base, const so3g_obs *obs, int n_obs,
                     const long long *work_off, long long n_work) {
     __shared__ int s_queue[QueueInts<C, P, MODE>::value];
