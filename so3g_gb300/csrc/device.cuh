@@ -285,6 +285,21 @@ __device__ __forceinline__ long long hp_ang2pix(long long nside, bool nest, doub
     return hp_hpd2pix(nside, nest, f, ix, iy);
 }
 
+// Tile and in-tile index of a HEALPix NEST pixel ip >= 0 with nppt pixels
+// per tile: a power of 4 for the power-of-2 nside and nside_tile the
+// pixelizor accepts, split with a shift and a mask instead of a 64-bit
+// division; a division otherwise.
+__device__ __forceinline__ void hp_tile_split(long long nppt, long long ip, int &tile, int &sub) {
+    if ((nppt & (nppt - 1)) == 0) {
+        const int s = __ffsll(nppt) - 1;
+        tile = (int)(ip >> s);
+        sub = (int)(ip & (nppt - 1));
+    } else {
+        tile = (int)(ip / nppt);
+        sub = (int)(ip - (long long)tile * nppt);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Pixelizors.  get_pixel() is GetPixel (used by pixels/pointing_matrix:
 // writes only the slots it sets); get_pixels() is GetPixels (interpolation
@@ -304,8 +319,7 @@ __device__ __forceinline__ bool get_pixel(const DGeom &g, const double *coords, 
             return true;
         }
         if (ix < 0) { idx[0] = -1; return false; }
-        idx[0] = (int)(ix / g.nppt);
-        idx[1] = (int)(ix % g.nppt);
+        hp_tile_split(g.nppt, ix, idx[0], idx[1]);
         return true;
     }
     // Pixelizor2_Flat<NonTiled>::GetPixel :845-863 / <Tiled> :1029-1051
@@ -339,8 +353,7 @@ __device__ __forceinline__ int get_pixels(const DGeom &g, const double *coords, 
         if (P == PX_HP_NT) {
             pix[0][0] = (int)ix;
         } else {
-            pix[0][0] = (int)(ix / g.nppt);
-            pix[0][1] = (int)(ix % g.nppt);
+            hp_tile_split(g.nppt, ix, pix[0][0], pix[0][1]);
         }
         w[0] = 1;
         return 1;

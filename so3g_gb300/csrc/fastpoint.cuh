@@ -580,8 +580,7 @@ __device__ __forceinline__ bool fast_healpix(const DGeom &g, const FastTables &f
     if (P == PX_HP_NT) {
         pix[0][0] = (int)ip;
     } else {
-        pix[0][0] = (int)(ip / g.nppt);
-        pix[0][1] = (int)(ip % g.nppt);
+        hp_tile_split(g.nppt, ip, pix[0][0], pix[0][1]);
     }
     n = 1;
     return true;

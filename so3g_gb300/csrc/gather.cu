@@ -63,8 +63,7 @@ __global__ void k_map_f32_tiled(DGeom g, const double *map, long long npix, floa
     if (i >= npix) return;
     int pix[3];
     if (P == PX_HP_T) {
-        pix[0] = (int)(i / g.nppt);
-        pix[1] = (int)(i - (long long)pix[0] * g.nppt);
+        hp_tile_split(g.nppt, i, pix[0], pix[1]);
         pix[2] = 0;
     } else {
         const int gy = (int)(i / g.nx), gx = (int)(i - (long long)gy * g.nx);

@@ -454,8 +454,7 @@ __device__ __forceinline__ bool mixed_healpix(const DGeom &g, const FastTables &
     if (P == PX_HP_NT) {
         pix[0] = (int)ip;
     } else {
-        pix[0] = (int)(ip / g.nppt);
-        pix[1] = (int)(ip % g.nppt);
+        hp_tile_split(g.nppt, ip, pix[0], pix[1]);
     }
     if (SPIN) mixed_spin(o, nc, T, Pr, pf);
     return true;
