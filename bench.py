@@ -79,7 +79,8 @@ def parse():
                     help="operations timed in a step (profiling runs pick one)")
     ap.add_argument("--batch-scale", type=float, default=1.0,
                     help="cfg4: scale every observation's sample count")
-    ap.add_argument("--tiled", action="store_true", help="cfg3: the Tiled NEST variant")
+    ap.add_argument("--tiled", action="store_true",
+                    help="cfg3: the Tiled NEST variant; cfg1/cfg2: 100x100 tiles")
     ap.add_argument("--pointing", default="mixed", choices=["mixed", "certified", "exact"],
                     help="pointing mode of the timed steps")
     ap.add_argument("--precomp", action="store_true",
@@ -94,7 +95,7 @@ def config(args):
         c["n_det"] = args.n_det
     if args.n_time:
         c["n_time"] = args.n_time
-    if args.tiled and c["kind"] == "hp":
+    if args.tiled and c["kind"] in ("hp", "car"):
         c["tiled"] = True
     return c
 
@@ -115,7 +116,8 @@ def describe(c):
         return ("differentiable from_map forward+backward TOD samples/s (ZEA bilinear TQU)",
                 "ZEA bilinear TQU NonTiled %dx%d float64 map, %s" % (shape[0], shape[1], n),
                 [3] + shape)
-    return (METRIC, "CAR TQU NonTiled %dx%d float64 map, %s" % (shape[0], shape[1], n),
+    tiling = "Tiled (100x100 tiles, all present)" if c.get("tiled") else "NonTiled"
+    return (METRIC, "CAR TQU %s %dx%d float64 map, %s" % (tiling, shape[0], shape[1], n),
             [3] + shape)
 
 
@@ -171,7 +173,8 @@ def host_inputs(c, seed=0):
                                     proj="ZEA", interpol="bilinear")
     else:
         p = synth.car_projectionist(c["shape"], c.get("res_arcmin", 1.) * ARCMIN, el=el,
-                                    az0=180., proj=c.get("proj", "CAR"))
+                                    az0=180., proj=c.get("proj", "CAR"),
+                                    tile_shape=(100, 100) if c.get("tiled") else None)
     q = synth.native(p, Q)
     return p, q, dets, resp
 
@@ -450,7 +453,7 @@ def run_ours(args, c, rank, world):
         e1.record(stream)
         torch.cuda.synchronize()
         res["to_weight_map_ms"] = e0.elapsed_time(e1)
-    if not args.no_e2e and world == 1 and c["kind"] == "car":
+    if not args.no_e2e and world == 1 and c["kind"] == "car" and not c.get("tiled"):
         res["e2e"] = run_e2e(args, c, eng, q, dets, resp, sig, dev)
     del sig, out
     return res, N
@@ -903,7 +906,7 @@ def main():
             "roofline": {"bound": "hbm", "kernel": op, "achieved": achieved, "peak": hbm,
                          "unit": "GB/s", "frac": achieved / hbm,
                          "traffic": (MEASURED_TRAFFIC_PER_SAMPLE[args.pointing][op] * N
-                                     if c["kind"] == "car" and op in
+                                     if c["kind"] == "car" and not c.get("tiled") and op in
                                      MEASURED_TRAFFIC_PER_SAMPLE.get(args.pointing, {})
                                      else None),
                          "bytes_per_sample": B, "peak_kind": kind},
@@ -931,7 +934,7 @@ def main():
                                  "samples_per_s": N / (res["to_weight_map_ms"] * 1e-3)}
     if "e2e" in res:
         line["e2e"] = res["e2e"]
-    if world == 1 and c["kind"] == "car" and not args.no_precomp:
+    if world == 1 and c["kind"] == "car" and not c.get("tiled") and not args.no_precomp:
         # The same workload with its pointing precomputed once
         # (ProjEng_Precomp): the HBM-bound form of the path.
         r = precomp_leg(c, args.steps, args.warmup)

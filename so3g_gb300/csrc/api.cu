@@ -249,6 +249,9 @@ int make_geom_lut(const so3g_pixelization *pz, DGeom *g, const double *lut) {
         g->ntx = (g->nx + g->tx - 1) / g->tx;
         g->n_tile = g->nty * g->ntx;
         if (g->ntx == 0) g->ntx = 1;  // empty map: keeps the tile arithmetic defined
+        g->inv_ty = 1.0f / (float)g->ty;
+        g->inv_tx = 1.0f / (float)g->tx;
+        g->inv_ntx = 1.0f / (float)g->ntx;
     }
     return SO3G_OK;
 }

@@ -41,6 +41,7 @@ struct DGeom {
     double cry, crx;         // crpix (y, x)
     int ty, tx;              // Flat tile shape
     int nty, ntx;            // Flat tile grid
+    float inv_ty, inv_tx, inv_ntx;   // their reciprocals (div_small)
     long long nside, npix;   // HEALPix
     long long nppt;          // HEALPix pixels per tile
     int n_tile;              // tiles of the pixelization (0 untiled)
@@ -285,6 +286,27 @@ __device__ __forceinline__ long long hp_ang2pix(long long nside, bool nest, doub
     return hp_hpd2pix(nside, nest, f, ix, iy);
 }
 
+// x / d for 0 <= x < 2^24 and 1 <= d < 2^24 from inv_d = 1/d rounded to
+// float32: x * inv_d is within one of the quotient (relative error below
+// 2^-23, and exact for d = 1), which one remainder test corrects -- a few
+// instructions instead of an integer division.
+__device__ __forceinline__ int div_small(int x, int d, float inv_d) {
+    if (x >= (1 << 24)) return x / d;
+    int q = __float2int_rz(__int2float_rn(x) * inv_d);
+    const int r = x - q * d;
+    q += (r >= d) - (r < 0);
+    return q;
+}
+
+// Tile tuple (tile, row and column in the tile) of parent-map pixel
+// (iy, ix) >= 0 of a flat tiled pixelizor (:1029-1051, :1124-1138).
+__device__ __forceinline__ void flat_tile_tuple(const DGeom &g, int iy, int ix, int *t) {
+    const int sub_y = div_small(iy, g.ty, g.inv_ty), sub_x = div_small(ix, g.tx, g.inv_tx);
+    t[0] = sub_y * g.ntx + sub_x;
+    t[1] = iy - sub_y * g.ty;
+    t[2] = ix - sub_x * g.tx;
+}
+
 // Tile and in-tile index of a HEALPix NEST pixel ip >= 0 with nppt pixels
 // per tile: a power of 4 for the power-of-2 nside and nside_tile the
 // pixelizor accepts, split with a shift and a mask instead of a 64-bit
@@ -331,11 +353,7 @@ __device__ __forceinline__ bool get_pixel(const DGeom &g, const double *coords, 
         idx[0] = int(iy);
         idx[1] = int(ix);
     } else {
-        int sub_y = int(iy) / g.ty;
-        int sub_x = int(ix) / g.tx;
-        idx[0] = sub_y * g.ntx + sub_x;
-        idx[1] = int(iy) - sub_y * g.ty;
-        idx[2] = int(ix) - sub_x * g.tx;
+        flat_tile_tuple(g, int(iy), int(ix), idx);
     }
     return true;
 }
@@ -374,11 +392,7 @@ __device__ __forceinline__ int get_pixels(const DGeom &g, const double *coords, 
         if (!(x > -1 && x < g.nx)) return 0;
         if (!(y > -1 && y < g.ny)) return 0;
         int ix = int(x), iy = int(y);
-        int sub_y = iy / g.ty;
-        int sub_x = ix / g.tx;
-        pix[0][0] = sub_y * g.ntx + sub_x;
-        pix[0][1] = iy - sub_y * g.ty;
-        pix[0][2] = ix - sub_x * g.tx;
+        flat_tile_tuple(g, iy, ix, pix[0]);
         w[0] = 1;
         return 1;
     } else {
@@ -407,10 +421,7 @@ __device__ __forceinline__ int get_pixels(const DGeom &g, const double *coords, 
                     pix[iout][0] = iy;
                     pix[iout][1] = ix;
                 } else {
-                    int sub_y = iy / g.ty, sub_x = ix / g.tx;
-                    pix[iout][0] = sub_y * g.ntx + sub_x;
-                    pix[iout][1] = iy - sub_y * g.ty;
-                    pix[iout][2] = ix - sub_x * g.tx;
+                    flat_tile_tuple(g, iy, ix, pix[iout]);
                 }
                 w[iout] = wy[dy] * wx[dx];
                 iout++;
@@ -442,7 +453,7 @@ __device__ __forceinline__ int locate(const DGeom &g, const int *idx, long long 
             *off = toff + idx[1];
             *plane = g.nppt;
         } else {
-            int row = t / g.ntx, col = t - (t / g.ntx) * g.ntx;
+            const int row = div_small(t, g.ntx, g.inv_ntx), col = t - row * g.ntx;
             long long tny = min(g.ty, g.ny - row * g.ty);
             long long tnx = min(g.tx, g.nx - col * g.tx);
             *off = toff + idx[1] * tnx + idx[2];

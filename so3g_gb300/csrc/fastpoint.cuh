@@ -354,10 +354,7 @@ __device__ __forceinline__ bool fast_pixels(const DGeom &g, dfl x, dfl y, int (*
         // :1124-1138 (int() truncation: x in (-1, 0) lands in column 0)
         const int tx = (x.hi < 0.f) ? ix + 1 : ix, ty = (y.hi < 0.f) ? iy + 1 : iy;
         if (tx >= 0 && tx < g.nx && ty >= 0 && ty < g.ny) {
-            const int sub_y = ty / g.ty, sub_x = tx / g.tx;
-            pix[0][0] = sub_y * g.ntx + sub_x;
-            pix[0][1] = ty - sub_y * g.ty;
-            pix[0][2] = tx - sub_x * g.tx;
+            flat_tile_tuple(g, ty, tx, pix[0]);
             w[0] = 1.f;
             n = 1;
         }
@@ -390,10 +387,7 @@ __device__ __forceinline__ bool fast_pixels(const DGeom &g, dfl x, dfl y, int (*
                     pix[n][0] = yy;
                     pix[n][1] = xx;
                 } else {
-                    const int sub_y = yy / g.ty, sub_x = xx / g.tx;
-                    pix[n][0] = sub_y * g.ntx + sub_x;
-                    pix[n][1] = yy - sub_y * g.ty;
-                    pix[n][2] = xx - sub_x * g.tx;
+                    flat_tile_tuple(g, yy, xx, pix[n]);
                 }
                 w[n] = df_mul(wy[dy], wx[dx]).hi;
                 n++;

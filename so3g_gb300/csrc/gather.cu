@@ -48,7 +48,7 @@ constexpr long long kMap32TiledMaxPixels = 1LL << 28;
 template <int P>
 __device__ __forceinline__ long long map32_index(const DGeom &g, const int *pix, long long off) {
     if (P == PX_FLAT_T_NN || P == PX_FLAT_T_BL) {
-        const int t = pix[0], row = t / g.ntx, col = t - row * g.ntx;
+        const int t = pix[0], row = div_small(t, g.ntx, g.inv_ntx), col = t - row * g.ntx;
         return (long long)(row * g.ty + pix[1]) * g.nx + (long long)col * g.tx + pix[2];
     }
     if (P == PX_HP_T) return (long long)pix[0] * g.nppt + pix[1];
@@ -67,10 +67,7 @@ __global__ void k_map_f32_tiled(DGeom g, const double *map, long long npix, floa
         pix[2] = 0;
     } else {
         const int gy = (int)(i / g.nx), gx = (int)(i - (long long)gy * g.nx);
-        const int row = gy / g.ty, col = gx / g.tx;
-        pix[0] = row * g.ntx + col;
-        pix[1] = gy - row * g.ty;
-        pix[2] = gx - col * g.tx;
+        flat_tile_tuple(g, gy, gx, pix);
     }
     float v[3] = {0.f, 0.f, 0.f};
     long long off, plane;

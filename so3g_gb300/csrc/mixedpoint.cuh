@@ -270,10 +270,7 @@ __device__ __forceinline__ bool mixed_flat_pixel(const DGeom &g, const MixedCons
         const int tx = (x < 0.f) ? ix + 1 : ix, ty = (y < 0.f) ? iy + 1 : iy;
         on = tx >= 0 && tx < g.nx && ty >= 0 && ty < g.ny && x > -1.f && y > -1.f;
         if (on) {
-            const int sub_y = ty / g.ty, sub_x = tx / g.tx;
-            pix[0] = sub_y * g.ntx + sub_x;
-            pix[1] = ty - sub_y * g.ty;
-            pix[2] = tx - sub_x * g.tx;
+            flat_tile_tuple(g, ty, tx, pix);
         }
     }
     return true;
