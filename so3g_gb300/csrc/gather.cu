@@ -55,8 +55,19 @@ __device__ __forceinline__ long long map32_index(const DGeom &g, const int *pix,
     return off;
 }
 
-// The float32 copy of a tiled map over its parent map's pixels (absent
-// tiles: zeros, never read -- their samples raise the missing-tile error).
+// Tile tuple of a parent-map pixel in the float32 tier's PARENT form.
+template <int P>
+__device__ __forceinline__ void parent_to_tile(const DGeom &g, const int *par, int *tp) {
+    if (P == PX_HP_T) {
+        hp_tile_split(g.nppt, par[0], tp[0], tp[1]);
+    } else {
+        flat_tile_tuple(g, par[0], par[1], tp);
+    }
+}
+
+// The float32 copy of a tiled map over its parent map's pixels, .w = 1 on
+// present tiles and 0 on absent ones (whose samples raise the missing-tile
+// error).
 template <int P>
 __global__ void k_map_f32_tiled(DGeom g, const double *map, long long npix, float4 *out) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -71,10 +82,11 @@ __global__ void k_map_f32_tiled(DGeom g, const double *map, long long npix, floa
     }
     float v[3] = {0.f, 0.f, 0.f};
     long long off, plane;
-    if (locate<P>(g, pix, &off, &plane) < 0)
+    const bool present = locate<P>(g, pix, &off, &plane) < 0;
+    if (present)
         for (int c = 0; c < g.ncomp && c < 3; c++)
             v[c] = __double2float_rn(__ldg(map + off + c * plane));
-    out[i] = make_float4(v[0], v[1], v[2], 0.f);
+    out[i] = make_float4(v[0], v[1], v[2], present ? 1.f : 0.f);
 }
 
 // The untiled map's components as float32, pixel by pixel (one 16-byte
@@ -345,8 +357,32 @@ __global__ void __launch_bounds__(kBlock, MixedEligible<C, P>::value && MODE == 
                 int pix[3];
                 float pf[3];
                 bool on = false;
-                if (mixed_pointing<C, P>(a.g, a.ft, a.mc, qb, qd32, nc, T, Pr, pix, on, pf)) {
-                    if (on) {
+                // Tiled maps: the pixel comes as a parent-map index; with the
+                // float32 copy (indexed by it, tile presence in .w) no tile
+                // arithmetic is needed.
+                constexpr bool kParent = P == PX_FLAT_T_NN || P == PX_HP_T;
+                if (mixed_pointing<C, P, true, kParent>(a.g, a.ft, a.mc, qb, qd32, nc, T, Pr, pix,
+                                                        on, pf)) {
+                    if (kParent && on && a.map32) {
+                        const long long gi = P == PX_HP_T
+                                                 ? (long long)pix[0]
+                                                 : (long long)pix[0] * a.g.nx + pix[1];
+                        const float4 m = __ldg(a.map32 + gi);
+                        if (m.w != 0.f) {
+                            float s = fmaf(m.x, pf[0], s_in);
+                            if (nc > 1) s = fmaf(m.y, pf[1], s);
+                            if (nc > 2) s = fmaf(m.z, pf[2], s);
+                            *sp = s;
+                        } else {
+                            int tp[3];
+                            parent_to_tile<P>(a.g, pix, tp);
+                            record_missing_tile(a.err, tp[0]);
+                        }
+                    } else if (on) {
+                        if (kParent) {
+                            const int par[2] = {pix[0], pix[1]};
+                            parent_to_tile<P>(a.g, par, pix);
+                        }
                         long long off, plane;
                         const int bad = locate<P>(a.g, pix, &off, &plane);
                         if (bad >= 0) {

@@ -247,8 +247,9 @@ __device__ __forceinline__ bool floor_cert(float v, float e, int &i) {
 // cdx + crpix_x - 1 + 0.5 (and y) from projection-plane coordinates (X, Y)
 // with error bounds (eX, eY), the float32 roundings of 1/cdx, of the offset
 // and of the fma added, x1.5 safety; false when an integer part is not
-// certain.
-template <int P>
+// certain.  PARENT (tiled): the pixel's parent-map coordinates (iy, ix) in
+// pix[0..1] instead of its tile tuple.
+template <int P, bool PARENT = false>
 __device__ __forceinline__ bool mixed_flat_pixel(const DGeom &g, const MixedConst &mc, float X,
                                                  float Y, float eX, float eY, int *pix,
                                                  bool &on) {
@@ -270,7 +271,12 @@ __device__ __forceinline__ bool mixed_flat_pixel(const DGeom &g, const MixedCons
         const int tx = (x < 0.f) ? ix + 1 : ix, ty = (y < 0.f) ? iy + 1 : iy;
         on = tx >= 0 && tx < g.nx && ty >= 0 && ty < g.ny && x > -1.f && y > -1.f;
         if (on) {
-            flat_tile_tuple(g, ty, tx, pix);
+            if (PARENT) {
+                pix[0] = ty;
+                pix[1] = tx;
+            } else {
+                flat_tile_tuple(g, ty, tx, pix);
+            }
         }
     }
     return true;
@@ -278,14 +284,15 @@ __device__ __forceinline__ bool mixed_flat_pixel(const DGeom &g, const MixedCons
 
 // The float32 tier for CAR with a nearest-neighbour flat pixelizor.
 // Returns false when the sample must go to the double-float path.
-template <int P, bool SPIN>
+template <int P, bool SPIN, bool PARENT>
 __device__ __forceinline__ bool mixed_car(const DGeom &g, const FastTables &ft,
                                           const MixedConst &mc, const float (&qb)[4],
                                           const float (&qd)[4], int nc, float T, float Pr,
                                           int *pix, bool &on, float *pf) {
     MixedLonLat o;
     if (!mixed_lonlat(ft, mc, qb, qd, o)) return false;
-    if (!mixed_flat_pixel<P>(g, mc, o.lon, o.lat, o.elon, o.elat, pix, on)) return false;
+    if (!mixed_flat_pixel<P, PARENT>(g, mc, o.lon, o.lat, o.elon, o.elat, pix, on))
+        return false;
     if (SPIN && on) mixed_spin(o, nc, T, Pr, pf);
     return true;
 }
@@ -300,7 +307,7 @@ __device__ __forceinline__ bool mixed_car(const DGeom &g, const FastTables &ft,
 // +- 20u scales u, v and n; plus the float32 roundings.  False (double-
 // float path) far from the projection's pole: TAN with cos(theta) < 0.1,
 // ZEA and SIN with n < 0.25 (theta > 120 deg).
-template <int C, int P, bool SPIN>
+template <int C, int P, bool SPIN, bool PARENT>
 __device__ __forceinline__ bool mixed_zen(const DGeom &g, const MixedConst &mc,
                                           const float (&qb)[4], const float (&qd)[4], int nc,
                                           float T, float Pr, int *pix, bool &on, float *pf) {
@@ -336,7 +343,7 @@ __device__ __forceinline__ bool mixed_zen(const DGeom &g, const MixedConst &mc,
         // absolute rounding, <= u) + |P| (10u: norm, 6u: roundings).
         e = fmaf(22.f * kU, r, 16.f * kU * (fabsf(X) + fabsf(Y)));
     }
-    if (!mixed_flat_pixel<P>(g, mc, X, Y, e, e, pix, on)) return false;
+    if (!mixed_flat_pixel<P, PARENT>(g, mc, X, Y, e, e, pix, on)) return false;
     if (!on || !SPIN) return true;
     // Spin factors (:1180-1209) with c = (a^2 - d^2)/n, s = 2ad/n.
     if (nc == 1) {
@@ -365,7 +372,7 @@ __device__ __forceinline__ bool mixed_zen(const DGeom &g, const MixedConst &mc,
 // <= 2^-21.41 for |lat| <= pi), every integer decision certified against
 // the propagated error bound (x1.5 safety).  Returns false when the sample
 // must go to the double-float path; the pixel is always on the map.
-template <int P, bool SPIN>
+template <int P, bool SPIN, bool PARENT>
 __device__ __forceinline__ bool mixed_healpix(const DGeom &g, const FastTables &ft,
                                               const MixedConst &mc, const float (&qb)[4],
                                               const float (&qd)[4], int nc, float T, float Pr,
@@ -448,7 +455,7 @@ __device__ __forceinline__ bool mixed_healpix(const DGeom &g, const FastTables &
     }
     const long long ip = hp_hpd2pix(nside, P == PX_HP_T ? true : (g.nest != 0), f, ix, iy);
     if (ip < 0 || ip >= g.npix) return false;
-    if (P == PX_HP_NT) {
+    if (P == PX_HP_NT || PARENT) {
         pix[0] = (int)ip;
     } else {
         hp_tile_split(g.nppt, ip, pix[0], pix[1]);
@@ -459,19 +466,21 @@ __device__ __forceinline__ bool mixed_healpix(const DGeom &g, const FastTables &
 
 // The float32 tier of one sample for pixelization P: one tap (weight 1)
 // when `on`.  False hands the sample to the double-float path.  SPIN =
-// false: the pixel only (the caller forms certified spin factors).
-template <int C, int P, bool SPIN = true>
+// false: the pixel only (the caller forms certified spin factors).  PARENT
+// (tiled pixelizors): the pixel as a parent-map index -- flat (iy, ix) in
+// pix[0..1], HEALPix the NEST index in pix[0] -- instead of a tile tuple.
+template <int C, int P, bool SPIN = true, bool PARENT = false>
 __device__ __forceinline__ bool mixed_pointing(const DGeom &g, const FastTables &ft,
                                                const MixedConst &mc, const float (&qb)[4],
                                                const float (&qd)[4], int nc, float T, float Pr,
                                                int *pix, bool &on, float *pf) {
     if (P == PX_HP_NT || P == PX_HP_T) {
         on = true;
-        return mixed_healpix<P, SPIN>(g, ft, mc, qb, qd, nc, T, Pr, pix, pf);
+        return mixed_healpix<P, SPIN, PARENT>(g, ft, mc, qb, qd, nc, T, Pr, pix, pf);
     }
     if (C == SO3G_COORD_CAR)
-        return mixed_car<P, SPIN>(g, ft, mc, qb, qd, nc, T, Pr, pix, on, pf);
-    return mixed_zen<C, P, SPIN>(g, mc, qb, qd, nc, T, Pr, pix, on, pf);
+        return mixed_car<P, SPIN, PARENT>(g, ft, mc, qb, qd, nc, T, Pr, pix, on, pf);
+    return mixed_zen<C, P, SPIN, PARENT>(g, mc, qb, qd, nc, T, Pr, pix, on, pf);
 }
 
 }  // namespace so3g

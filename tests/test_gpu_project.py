@@ -187,8 +187,10 @@ def test_thread_intervals_shape_errors(orc, gpulib):
         c.eng.to_map(None, c.bore, c.dets, c.resp, c.signal, None, bad_time)
 
 
-def test_missing_tile_raises(orc, gpulib):
+@pytest.mark.parametrize("mode", MODES)
+def test_missing_tile_raises(orc, gpulib, mode):
     c = Case(orc, coord="CAR", tiled=True, n_det=4, n_time=3000)
+    c.eng.pointing = mode
     hits = np.array(c.eng.tile_hits(c.bore, c.dets))
     hit = np.nonzero(hits)[0]
     assert len(hit) > 1
@@ -198,7 +200,7 @@ def test_missing_tile_raises(orc, gpulib):
     m = c.blank((3,), populate=pop)
     with pytest.raises(RuntimeError, match=r"Tiling problem \(index %d\)" % hit[0]):
         c.eng.to_map(m, c.bore, c.dets, c.resp, c.signal, None, None)
-    with pytest.raises(RuntimeError, match="Tiling problem"):
+    with pytest.raises(RuntimeError, match=r"Tiling problem \(index %d\)" % hit[0]):
         c.eng.from_map(c.random_map((3,), populate=pop), c.bore, c.dets, c.resp, None)
 
 
