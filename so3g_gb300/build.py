@@ -23,9 +23,10 @@ LIB = os.path.join(LIBDIR, LIBNAME)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC",
               "-Xptxas", "-warn-spills"]
-UNITS = ["api.cu", "pointing.cu", "scatter.cu", "gather.cu", "precomp.cu", "noalloc.cu", "batch.cu",
-         "sightline.cu", "ranges.cu"]
-HEADERS = ["device.cuh", "host.h", "scatter_kernel.cuh", "fastpoint.cuh", "mixedpoint.cuh"]
+UNITS = ["api.cu", "pointing.cu", "scatter.cu", "scatter_weight.cu", "gather.cu", "precomp.cu",
+         "noalloc.cu", "batch.cu", "batch_weight.cu", "sightline.cu", "ranges.cu"]
+HEADERS = ["device.cuh", "host.h", "scatter_kernel.cuh", "scatter_launch.cuh", "batch_launch.cuh",
+           "fastpoint.cuh", "mixedpoint.cuh"]
 
 
 def nvcc():
