@@ -766,9 +766,11 @@ def cpu_sample(c, n_det_s, n_time_s):
     return s
 
 
-def run_cpu(c, n_det_s, n_time_s, steps=1, threads=None):
+def run_cpu(c, n_det_s, n_time_s, steps=1, threads=None, assign=True):
     """to_map (+ 'simple' thread assignment, reported apart) and from_map
-    of the oracle on a slice of the workload; returns samples/s."""
+    of the oracle on a slice of the workload; returns samples/s.  assign =
+    False: to_map with thread_intervals=None, the reference's default (one
+    thread); from_map keeps its threads over detectors."""
     from oracle import Oracle
     orc = Oracle()
     nthreads = threads or os.cpu_count() or 1
@@ -782,9 +784,11 @@ def run_cpu(c, n_det_s, n_time_s, steps=1, threads=None):
     sig = rng.standard_normal((n_det_s, n_time_s), dtype=np.float32)
     npix = npix_of(c)
     t0 = time.perf_counter()
-    lab = orc.labels(pz, q, dets, 0, nthreads)
+    threads_ranges = None
+    if assign:
+        lab = orc.labels(pz, q, dets, 0, nthreads)
+        threads_ranges = _labels_to_threads(lab, nthreads)
     t_assign = time.perf_counter() - t0
-    threads_ranges = _labels_to_threads(lab, nthreads)
     best = None
     for _ in range(steps):
         m = np.zeros(3 * npix)
@@ -948,9 +952,14 @@ def main():
     if world == 1 and not args.no_cpu:
         nd, nt = cpu_sample_size(c)
         r = run_cpu(c, nd, nt)
+        r1 = run_cpu(c, nd, nt, assign=False)
         line["cpu_baseline"] = {"value": r["value"], "unit": "samples/s", "cores": r["threads"],
                                 "kind": "port", "sample": r["sample"] + "; to_map with "
-                                "'simple' thread assignment (assignment not timed)"}
+                                "'simple' thread assignment (assignment not timed)",
+                                "value_default_threads": r1["value"],
+                                "default_threads": "to_map with thread_intervals=None (one "
+                                                   "thread, the reference's default), "
+                                                   "from_map over %d threads" % r1["threads"]}
     print(json.dumps(line))
 
 
