@@ -488,9 +488,11 @@ def run_e2e(args, c, eng, q, dets, resp, sig_dev, dev):
     for _ in range(max(3, args.warmup)):
         step()
     torch.cuda.synchronize()
-    # The host link of these shared hosts stalls now and then for 30-200 ms
-    # (plain torch copies show the same), so every step is timed on its own
-    # and the median step is the value; the mean is reported beside it.
+    # Every step is timed on its own.  The value is the mean step (all the
+    # timed steps' wall time over their count): the host link of these
+    # shared hosts stalls now and then for 30-200 ms (plain torch copies
+    # show the same), and those stalls are part of what a caller sees.  The
+    # median step, without them, is reported beside it.
     steps = max(3, args.steps)
     for v in parts.values():
         v.clear()
@@ -500,7 +502,7 @@ def run_e2e(args, c, eng, q, dets, resp, sig_dev, dev):
         step()
         torch.cuda.synchronize()
         per_step.append(time.perf_counter() - t0)
-    dt = float(np.median(per_step))
+    dt = float(np.mean(per_step))
     N = c["n_det"] * c["n_time"]
     nb_sig = sig_h.numel() * 4
     nb_map = m_h.numel() * 8
@@ -512,9 +514,9 @@ def run_e2e(args, c, eng, q, dets, resp, sig_dev, dev):
     from so3g_gb300 import projeng
     return {"value": N / dt, "unit": "samples/s", "h2d_bytes_per_step": int(h2d),
             "d2h_bytes_per_step": int(d2h), "ms_per_step": dt * 1e3,
-            "ms_per_step_mean": float(np.mean(per_step)) * 1e3,
+            "ms_per_step_median": float(np.median(per_step)) * 1e3,
             "ms_steps": [round(x * 1e3, 2) for x in per_step],
-            "estimator": "median of %d individually timed steps" % steps,
+            "estimator": "mean of %d individually timed steps" % steps,
             "op_ms": {k: float(np.median(v)) for k, v in parts.items()},
             "step": "to_map(host map, page-locked host signal) + from_map(host map, "
                     "signal=None) -> new host signal",
@@ -760,50 +762,91 @@ def run_batch(args, c):
 # ---------------------------------------------------------------------------
 # CPU: the oracle (the reference's algorithm restated in C++ with OpenMP).
 
-def cpu_sample(c, n_det_s, n_time_s):
-    s = dict(c)
-    s["n_det"], s["n_time"] = n_det_s, n_time_s
-    return s
+def cpu_signal(c, seed=0):
+    """float32 N(0,1) TOD (+ 1/f noise, knee 1 Hz, alpha -2) on the host
+    (torch's CPU generator and FFT, all host threads)."""
+    import torch
+    g = torch.Generator()
+    g.manual_seed(seed)
+    sig = torch.randn((c["n_det"], c["n_time"]), generator=g, dtype=torch.float32)
+    if c.get("noise"):
+        f = torch.fft.rfftfreq(c["n_time"], d=1 / 200.)
+        amp = torch.sqrt(1 + (1.0 / torch.clamp(f, min=1e-12)) ** 2)
+        amp[0] = 0.
+        for a in range(0, c["n_det"], 64):
+            b = min(c["n_det"], a + 64)
+            w = torch.randn((b - a, c["n_time"]), generator=g, dtype=torch.float32)
+            sig[a:b] += torch.fft.irfft(torch.fft.rfft(w) * amp, n=c["n_time"]).float()
+    return sig.numpy()
 
 
-def run_cpu(c, n_det_s, n_time_s, steps=1, threads=None, assign=True):
-    """to_map (+ 'simple' thread assignment, reported apart) and from_map
-    of the oracle on a slice of the workload; returns samples/s.  assign =
-    False: to_map with thread_intervals=None, the reference's default (one
-    thread); from_map keeps its threads over detectors."""
-    from oracle import Oracle
-    orc = Oracle()
-    nthreads = threads or os.cpu_count() or 1
-    orc.set_threads(nthreads)
-    s = cpu_sample(c, n_det_s, n_time_s)
-    s["tiled"] = False        # the oracle runs the untiled map
-    p, q, dets, resp = host_inputs(s)
-    eng = p.get_ProjEng("TQU")
-    pz = eng._pz()
-    rng = np.random.default_rng(0)
-    sig = rng.standard_normal((n_det_s, n_time_s), dtype=np.float32)
-    npix = npix_of(c)
-    t0 = time.perf_counter()
-    threads_ranges = None
-    if assign:
-        lab = orc.labels(pz, q, dets, 0, nthreads)
-        threads_ranges = _labels_to_threads(lab, nthreads)
-    t_assign = time.perf_counter() - t0
-    best = None
-    for _ in range(steps):
-        m = np.zeros(3 * npix)
+def _simple_threads(orc, pz, q, dets, n_domain, chunk=50):
+    """The reference's 'simple' thread assignment (pixel_ranges with
+    n_domain stripes, src/Projection.cxx:1440-1541) as [parallel bunch,
+    serial bunch] of per-thread, per-detector interval lists, built
+    detector chunk by chunk (the labels of the whole workload would take
+    4 bytes per sample)."""
+    n_det = len(dets)
+    par = [[None] * n_det for _ in range(n_domain)]
+    ser = [[None] * n_det]
+    for a in range(0, n_det, chunk):
+        b = min(n_det, a + chunk)
+        lab = orc.labels(pz, q, np.ascontiguousarray(dets[a:b]), 0, n_domain)
+        th = _labels_to_threads(lab, n_domain)
+        for k in range(n_domain):
+            par[k][a:b] = th[0][k]
+        ser[0][a:b] = th[1][0]
+    return [par, ser]
+
+
+class CpuWorkload:
+    """The oracle (the reference's ProjectionEngine arithmetic restated in
+    C++ with OpenMP) on the whole workload, on all host cores."""
+
+    def __init__(self, c, threads=None):
+        from oracle import Oracle
+        self.orc = Oracle()
+        self.threads = threads or os.cpu_count() or 1
+        self.orc.set_threads(self.threads)
+        s = dict(c)
+        s["tiled"] = False        # the oracle runs the untiled map
+        self.c = s
+        p, self.q, self.dets, self.resp = host_inputs(s)
+        self.pz = p.get_ProjEng("TQU")._pz()
+        self.sig = cpu_signal(s)
+        self.npix = npix_of(c)
+        self.out = np.zeros((s["n_det"], s["n_time"]), np.float32)
+        self.m = np.zeros(3 * self.npix)
         t0 = time.perf_counter()
-        orc.to_map(pz, q, dets, resp, sig, None, m, threads=threads_ranges)
+        self.ranges = self.orc.schedule(
+            _simple_threads(self.orc, self.pz, self.q, self.dets, self.threads),
+            len(self.dets))
+        self.assign_s = time.perf_counter() - t0
+
+    def step(self, simple=True):
+        """to_map (with the 'simple' thread assignment, or thread_intervals
+        = None: one thread, the reference's default) + from_map (OpenMP over
+        detectors); returns the seconds of each."""
+        self.m[:] = 0
+        t0 = time.perf_counter()
+        self.orc.to_map(self.pz, self.q, self.dets, self.resp, self.sig, None, self.m,
+                        threads=self.ranges if simple else None)
         t1 = time.perf_counter()
-        out = np.zeros((n_det_s, n_time_s), np.float32)
-        orc.from_map(pz, q, dets, resp, m, out)
+        self.out[:] = 0
+        self.orc.from_map(self.pz, self.q, self.dets, self.resp, self.m, self.out)
         t2 = time.perf_counter()
-        if best is None or (t2 - t0) < best[0]:
-            best = (t2 - t0, t1 - t0, t2 - t1)
-    N = n_det_s * n_time_s
-    return {"value": N / best[0], "to_map_s": best[1], "from_map_s": best[2],
-            "assign_s": t_assign, "threads": nthreads, "samples": N,
-            "sample": "%d det x %d samples of the %s workload" % (n_det_s, n_time_s, "same")}
+        return t1 - t0, t2 - t1
+
+    @property
+    def samples(self):
+        return self.c["n_det"] * self.c["n_time"]
+
+    def describe(self):
+        return ("the whole workload (%d det x %d samples) per step; to_map with the "
+                "reference's 'simple' thread assignment over %d threads (assignment %.1f s, "
+                "made once, not timed), from_map over %d threads" % (
+                    self.c["n_det"], self.c["n_time"], self.threads, self.assign_s,
+                    self.threads))
 
 
 class _R:
@@ -837,11 +880,51 @@ def _labels_to_threads(lab, n_domain):
     return [[[_R(iv) for iv in th] for th in par], [[_R(iv) for iv in th] for th in ser]]
 
 
-def cpu_sample_size(c):
-    # About 10-30 s of CPU work across to_map + from_map.
-    n_det = min(c["n_det"], 100)
-    n_time = min(c["n_time"], 200_000)
-    return n_det, n_time
+def run_reference(args, c, cfg, metric, world):
+    """The reference arm: the oracle on the whole workload, W warm-up
+    steps, then K timed steps; the median step gives the value."""
+    w = CpuWorkload(c)
+    for _ in range(args.warmup):
+        w.step()
+    per = []
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        a, b = w.step()
+        per.append((time.perf_counter() - t0, a, b))
+    total = time.perf_counter() - t_all
+    ms = float(np.median([x[0] for x in per])) * 1e3
+    value = w.samples / (ms * 1e-3)
+    line = {"metric": metric, "value": value, "unit": "samples/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": cfg, "impl": "reference",
+            "op_ms": {"to_map": float(np.median([x[1] for x in per])) * 1e3,
+                      "from_map": float(np.median([x[2] for x in per])) * 1e3},
+            "ms_per_step_mean": total / max(1, args.steps) * 1e3,
+            "estimator": "median of %d steps after %d warm-up steps" % (args.steps, args.warmup),
+            "cpu_baseline": {"value": value, "unit": "samples/s", "cores": w.threads,
+                             "kind": "port", "sample": w.describe()},
+            "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def cpu_baseline(c):
+    """One step of the oracle on the whole workload with the 'simple'
+    thread assignment, and one with thread_intervals = None (to_map on one
+    thread, as the reference runs it by default)."""
+    w = CpuWorkload(c)
+    w.step()                                   # warm-up (page faults, caches)
+    a, b = w.step()
+    a1, b1 = w.step(simple=False)
+    return {"value": w.samples / (a + b), "unit": "samples/s", "cores": w.threads,
+            "kind": "port", "sample": w.describe() + "; one step after one warm-up step",
+            "op_s": {"to_map": a, "from_map": b},
+            "value_default_threads": w.samples / (a1 + b1),
+            "default_threads": "to_map with thread_intervals=None (one thread, the "
+                               "reference's default): %.1f s; from_map over %d threads" % (
+                                   a1, w.threads)}
 
 
 # ---------------------------------------------------------------------------
@@ -865,7 +948,10 @@ def main():
                  if c["kind"] == "zea_grad" else args.ops.replace(",", " + "))
     cfg = {"workload": workload, "n_det": c["n_det"], "n_time": c["n_time"],
            "map": map_shape, "step": step_name,
-           "l2": "inputs larger than L2 (TOD %.1f GB)" % (c["n_det"] * c["n_time"] * 4 / 1e9),
+           "l2": ("inputs larger than L2 (TOD %.1f GB)" % (c["n_det"] * c["n_time"] * 4 / 1e9)
+                  if c["n_det"] * c["n_time"] * 4 > 129e6 else
+                  "TOD of %.1f MB fits in L2 (no flush between steps)" % (
+                      c["n_det"] * c["n_time"] * 4 / 1e6)),
            "precision": (PRECISION[args.pointing] if c["kind"] in ("car", "hp") or
                          args.pointing != "mixed" else
                          "double-float pointing with the reference's bilinear taps (certified, "
@@ -877,21 +963,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        nd, nt = cpu_sample_size(c)
-        r = run_cpu(c, nd, nt, steps=max(1, args.steps))
-        line = {"metric": metric, "value": r["value"], "unit": "samples/s", "n_gpus": world,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step":
-                c["n_det"] * c["n_time"] / r["value"] * 1e3, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": cfg, "impl": "reference",
-                "cpu_baseline": {"value": r["value"], "unit": "samples/s",
-                                 "cores": r["threads"], "kind": "port",
-                                 "sample": r["sample"] + "; to_map with 'simple' thread "
-                                 "assignment (assignment %.2f s, not timed)" % r["assign_s"]},
-                "e2e": {"value": r["value"], "unit": "samples/s", "h2d_bytes_per_step": 0,
-                        "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
-        return
+        return run_reference(args, c, cfg, metric, world)
 
     res, N = run_ours(args, c, rank, world)
     if rank != 0:
@@ -950,16 +1022,7 @@ def main():
                                    "(pixel indices bit-exact, spin factors as the "
                                    "certified path)"}
     if world == 1 and not args.no_cpu:
-        nd, nt = cpu_sample_size(c)
-        r = run_cpu(c, nd, nt)
-        r1 = run_cpu(c, nd, nt, assign=False)
-        line["cpu_baseline"] = {"value": r["value"], "unit": "samples/s", "cores": r["threads"],
-                                "kind": "port", "sample": r["sample"] + "; to_map with "
-                                "'simple' thread assignment (assignment not timed)",
-                                "value_default_threads": r1["value"],
-                                "default_threads": "to_map with thread_intervals=None (one "
-                                                   "thread, the reference's default), "
-                                                   "from_map over %d threads" % r1["threads"]}
+        line["cpu_baseline"] = cpu_baseline(c)
     print(json.dumps(line))
 
 

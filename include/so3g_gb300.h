@@ -298,19 +298,22 @@ int so3g_proj_to_map(const so3g_pixelization *pz,
  * only pass buffers it already holds -- cannot provide the small device
  * tables so3g_proj_to_map needs besides its inputs and outputs, nor call the
  * allocating so3g_init().  This entry point keeps the error record, the trig
- * tables, the tile-offset table and the sample segments in one static device
- * array of 1.5 MiB per GPU (held until the process exits) and allocates
- * nothing.  Inputs, signal and map are device pointers as for
- * so3g_proj_to_map; the segments (host_seg: n_seg (det, start, end) int32
- * triples, or NULL for all samples) and the tile-offset table of a tiled map
- * (host_tile_offset: n_tile int64 element offsets, -1 = absent tile) are
- * HOST arrays, copied into the static array.  At most 65536 segments and
- * 65536 tiles; larger requests return SO3G_ERR_RANGE.  If host_err is not
- * NULL the call waits for the stream and copies the device error record
- * (as so3g_device_error) into it.  The first call on a device sets up the
- * static array (address lookup, trig-table upload): make it before any
- * stream capture.  All calls share the static array: calls that overlap on
- * the GPU race, so serialise them. */
+ * tables (with the double-float knots of the certified and mixed pointing),
+ * the tile-offset table and the sample segments in one static device array
+ * of 2.25 MiB per GPU (held until the process exits) and allocates nothing.
+ * Inputs, signal and map are device pointers as for so3g_proj_to_map; the
+ * pointing mode is pz->pointing, as there.  The segments (host_seg: n_seg
+ * (det, start, end) int32 triples, or NULL for all samples) and the
+ * tile-offset table of a tiled map (host_tile_offset: n_tile int64 element
+ * offsets, -1 = absent tile) are HOST arrays, copied into the static array;
+ * when either is given the call waits for the stream to consume them, so
+ * they may be reused on return.  At most 65536 segments and 65536 tiles;
+ * larger requests return SO3G_ERR_RANGE.  If host_err is not NULL the call
+ * waits for the stream and copies the device error record (as
+ * so3g_device_error) into it; otherwise so3g_noalloc_read_error reads it
+ * later.  Every call sets up the static array in the current CUDA context
+ * (address lookup, trig-table upload on `stream`).  All calls share the
+ * static array: calls that overlap on the GPU race, so serialise them. */
 int so3g_proj_to_map_noalloc(const so3g_pixelization *pz,
                              const double *boresight, int32_t n_time,
                              const double *dets, int32_t n_det,
@@ -321,6 +324,11 @@ int so3g_proj_to_map_noalloc(const so3g_pixelization *pz,
                              double *map_data,
                              const int64_t *host_tile_offset, int32_t n_tile,
                              int32_t accum, int32_t *host_err, void *stream);
+
+/* The device error record (as so3g_device_error) of the last
+ * so3g_proj_to_map_noalloc call on the current device, after waiting for
+ * `stream` (no counterpart in the reference; allocates nothing). */
+int so3g_noalloc_read_error(int32_t *host_err, void *stream);
 
 /* ProjectionEngine::to_weight_map (src/Projection.cxx:1968-2010, inner
  * loop :1813-1854): W[i, j, pix] += pf[i]*pf[j]*w*w*det_wt for j >= i. */

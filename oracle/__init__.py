@@ -63,7 +63,21 @@ def schedule(thread_intervals, n_det):
             np.asarray(toff, dtype=np.int32), np.asarray(boff, dtype=np.int32))
 
 
+class Schedule:
+    """A thread_intervals argument converted once (Oracle.schedule) for
+    repeated projections."""
+
+    def __init__(self, s, keep):
+        self.s = s
+        self.keep = keep
+
+
 class Oracle:
+    def schedule(self, threads, n_det):
+        """thread_intervals -> Schedule, accepted wherever `threads` is."""
+        s, keep = self._sched(threads, n_det)
+        return Schedule(s, keep)
+
     def __init__(self, threads=None):
         self.lib = ctypes.CDLL(_build.build_oracle())
         L = self.lib
@@ -206,6 +220,8 @@ class Oracle:
     def _sched(threads, n_det):
         if threads is None:
             return None, None
+        if isinstance(threads, Schedule):
+            return threads.s, threads.keep
         seg, toff, boff = schedule(threads, n_det)
         s = Sched()
         s.seg = _p(seg)

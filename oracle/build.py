@@ -15,7 +15,12 @@ import os
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE = os.environ.get("SO3G_REFERENCE", "/root/reference")
+# The so3g reference checkout: $SO3G_REFERENCE, else a checkout named
+# "reference" beside this repository's directory (absent on machines that
+# only run the tests; build_ref() then builds nothing).
+REFERENCE = os.environ.get(
+    "SO3G_REFERENCE",
+    os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 
 ORACLE_SO = os.path.join(HERE, "_build", "libproj_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libref_parts.so")

@@ -131,6 +131,7 @@ _SIGS = {
                                                 c_int32, c_void_p, c_void_p, c_int64, c_void_p,
                                                 c_void_p, c_int32, c_void_p, c_void_p, c_int32,
                                                 c_int32, c_void_p, c_void_p]),
+    "so3g_noalloc_read_error": (ctypes.c_int, [c_void_p, c_void_p]),
     "so3g_proj_to_weight_map": (ctypes.c_int, [P(Pixelization), c_void_p, c_int32, c_void_p,
                                                c_int32, c_void_p, c_void_p, P(Ranges), P(Map),
                                                c_int32, c_void_p, c_void_p]),

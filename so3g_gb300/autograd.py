@@ -10,9 +10,31 @@ to_map applied to the incoming signal gradient, so that
 and gradients of any loss of the projected signal flow back to the map.
 Both directions run the CUDA kernels of this package on the current
 stream.  Maps are untiled CUDA float64 tensors of shape (n_comp, ...); the
-signal is float32 (n_det, n_time).
+signal is float32 (n_det, n_time).  The engine's pointing mode is read once,
+in forward, and backward runs to_map in that same mode, so that the pair
+stays an adjoint pair even if the caller changes ``eng.pointing`` between
+the two.
 """
+import contextlib
+
 import torch
+
+from .projeng import DEFAULT_POINTING
+
+
+@contextlib.contextmanager
+def _pointing(eng, mode):
+    """Runs the block with ``eng.pointing = mode``, then restores it."""
+    had = "pointing" in vars(eng)
+    old = getattr(eng, "pointing", None)
+    eng.pointing = mode
+    try:
+        yield
+    finally:
+        if had:
+            eng.pointing = old
+        else:
+            del eng.pointing
 
 
 class FromMap(torch.autograd.Function):
@@ -26,6 +48,7 @@ class FromMap(torch.autograd.Function):
         if getattr(eng, "_tiled", False):
             raise TypeError("FromMap supports untiled maps only")
         ctx.eng = eng
+        ctx.mode = getattr(eng, "pointing", DEFAULT_POINTING)
         ctx.save_for_backward(boresight, dets, response)
         ctx.map_shape = tuple(map.shape)
         with torch.no_grad():
@@ -37,7 +60,8 @@ class FromMap(torch.autograd.Function):
         boresight, dets, response = ctx.saved_tensors
         g = grad_sig.detach().to(torch.float32).contiguous()
         gmap = torch.zeros(ctx.map_shape, dtype=torch.float64, device=g.device)
-        ctx.eng.to_map(gmap, boresight, dets, response, g, None, None)
+        with _pointing(ctx.eng, ctx.mode):
+            ctx.eng.to_map(gmap, boresight, dets, response, g, None, None)
         return gmap, None, None, None, None
 
 

@@ -63,6 +63,20 @@ void build_host_tables() {
     g_host_lut_ready = true;
 }
 
+// The knot tables of the certified pointing (asin, atan2, then sin/cos of
+// the asin knots), built once from the host tables.
+float4 g_host_knots[3 * kLutN];
+bool g_host_knots_ready = false;
+
+void build_host_knots() {
+    if (g_host_knots_ready) return;
+    build_host_tables();
+    fast_knots(g_host_lut, g_host_knots);
+    fast_knots(g_host_lut + kLutN, g_host_knots + kLutN);
+    sincos_knots(g_host_lut, g_host_knots + 2 * kLutN);
+    g_host_knots_ready = true;
+}
+
 bool pow2(long long v) { return v > 0 && (v & (v - 1)) == 0; }
 
 }  // namespace
@@ -187,6 +201,12 @@ const double *host_lut() {
     return g_host_lut;
 }
 
+const float4 *host_fast_knots() {
+    std::lock_guard<std::mutex> lk(g_mu);
+    build_host_knots();
+    return g_host_knots;
+}
+
 int make_geom(const so3g_pixelization *pz, DGeom *g) {
     const double *lut = device_lut();
     if (!lut) return set_error(SO3G_ERR_NOT_INIT, "so3g_init() was not called on this device");
@@ -301,14 +321,11 @@ int so3g_init(void) {
     }
     g_lut[dev] = d;
     // Double-float knots for the certified pointing.
-    static float4 knots[3 * kLutN];
-    fast_knots(g_host_lut, knots);
-    fast_knots(g_host_lut + kLutN, knots + kLutN);
-    sincos_knots(g_host_lut, knots + 2 * kLutN);
+    build_host_knots();
     float4 *f = nullptr;
     e = cudaMalloc(&f, sizeof(float4) * 3 * kLutN);
     if (e != cudaSuccess) return set_error(SO3G_ERR_CUDA, "cudaMalloc: %s", cudaGetErrorString(e));
-    e = cudaMemcpy(f, knots, sizeof(float4) * 3 * kLutN, cudaMemcpyHostToDevice);
+    e = cudaMemcpy(f, g_host_knots, sizeof(float4) * 3 * kLutN, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         cudaFree(f);
         return set_error(SO3G_ERR_CUDA, "cudaMemcpy: %s", cudaGetErrorString(e));

@@ -25,6 +25,10 @@ int make_geom(const so3g_pixelization *pz, DGeom *g);
 int make_geom_lut(const so3g_pixelization *pz, DGeom *g, const double *lut);
 // The host trig tables (asin then atan2, 2 x kLutN float64).
 const double *host_lut();
+// The host copy of the certified pointing's knot tables (asin, atan2, then
+// sin/cos of the asin knots: 3 x kLutN float4), the layout FastTables
+// points into.
+const float4 *host_fast_knots();
 // Double-float knot tables of the certified pointing on the current device
 // (uploaded by so3g_init), or NULL pointers.
 FastTables device_fast_tables();

@@ -16,17 +16,26 @@
 // arrays; the entry point copies them into the scratch before the launch.
 // It calls no cudaMalloc, cudaFree or other allocating routine.
 //
-// Set-up: the first call on a device, with that device current, looks up
-// the scratch's device address (cudaGetSymbolAddress) and copies the trig
-// tables into it.  Make that first call before any stream capture.
+// Set-up, on every call: the entry point looks up the scratch's device
+// address in the current context (cudaGetSymbolAddress) and copies the
+// trig tables (and, for the certified and mixed pointing, their
+// double-float knots) into it on the caller's stream, so a fresh context
+// (after cudaDeviceReset, or a caller's own CUDA context) is set up the
+// same way as the first one.  Pointing modes are those of so3g_proj_to_map
+// (pz->pointing); the mixed mode converts the float64 boresight itself, as
+// there is no room for its float32 copy.
+//
+// Host arrays: the segment and tile-offset tables are copied from the
+// caller's host arrays; the call waits for the stream to consume them, so
+// they may be reused or freed as soon as it returns.
 //
 // Sharing: every call uses the same scratch and leaves its contents there.
-// The error record is cleared at the start of each call; the tables are
-// rewritten.  Calls whose work overlaps on the GPU (different streams, or
-// different host threads) race on the scratch: serialise them.
+// The error record is cleared at the start of each call and can be read
+// afterwards with so3g_noalloc_read_error; the tables are rewritten.
+// Calls whose work overlaps on the GPU (different streams, or different
+// host threads) race on the scratch: serialise them.
 
 #include <climits>
-#include <mutex>
 
 #include "scatter_kernel.cuh"
 
@@ -38,41 +47,39 @@ namespace {
 constexpr int kNoAllocMaxTiles = 1 << 16;
 constexpr int kNoAllocMaxSegs = 1 << 16;
 
-// Scratch layout (byte offsets): error record, trig tables, tile offsets,
-// sample segments.  1.5 MiB in all.
+// Scratch layout (byte offsets): error record, trig tables, double-float
+// knot tables, tile offsets, sample segments.  2.25 MiB in all.
 constexpr size_t kOffErr = 0;
 constexpr size_t kOffLut = 256;
-constexpr size_t kOffTiles = kOffLut + sizeof(double) * 2 * kLutN;
+constexpr size_t kOffKnots = kOffLut + sizeof(double) * 2 * kLutN;
+constexpr size_t kOffTiles = kOffKnots + sizeof(float4) * 3 * kLutN;
 constexpr size_t kOffSegs = kOffTiles + sizeof(long long) * kNoAllocMaxTiles;
 constexpr size_t kScratchBytes = kOffSegs + 3 * sizeof(int) * kNoAllocMaxSegs;
+static_assert(kOffKnots % 16 == 0 && kOffTiles % 16 == 0, "scratch alignment");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mu;
-unsigned char *g_scratch_addr[kMaxDevices] = {nullptr};
-
-// Device address of the scratch on the current device; on the first call
-// per device also uploads the trig tables.
+// Device address of the scratch in the current context.
 int scratch_address(unsigned char **out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return set_error(SO3G_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
-    if (dev < 0 || dev >= kMaxDevices) return set_error(SO3G_ERR_RANGE, "device %d out of range", dev);
-    std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_addr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess)
-            return set_error(SO3G_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
-        unsigned char *base = static_cast<unsigned char *>(p);
-        e = cudaMemcpy(base + kOffLut, host_lut(), sizeof(double) * 2 * kLutN,
-                       cudaMemcpyHostToDevice);
-        if (e != cudaSuccess)
-            return set_error(SO3G_ERR_CUDA, "trig table upload: %s", cudaGetErrorString(e));
-        g_scratch_addr[dev] = base;
-    }
-    *out = g_scratch_addr[dev];
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess)
+        return set_error(SO3G_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    *out = static_cast<unsigned char *>(p);
+    return SO3G_OK;
+}
+
+// Copies the trig tables (and, for the certified and mixed pointing, the
+// knot tables) into the scratch on stream st.  The sources are the
+// library's static host tables, valid for the whole process.
+int upload_tables(unsigned char *scr, bool knots, cudaStream_t st) {
+    cudaError_t e = cudaMemcpyAsync(scr + kOffLut, host_lut(), sizeof(double) * 2 * kLutN,
+                                    cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && knots)
+        e = cudaMemcpyAsync(scr + kOffKnots, host_fast_knots(), sizeof(float4) * 3 * kLutN,
+                            cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess)
+        return set_error(SO3G_ERR_CUDA, "trig table upload: %s", cudaGetErrorString(e));
     return SO3G_OK;
 }
 
@@ -81,9 +88,18 @@ struct NoAllocLaunch {
     dim3 grid;
     cudaStream_t stream;
     template <int C, int P>
+    struct Go {
+        NoAllocLaunch *L;
+        template <int MODE>
+        int go() {
+            k_scatter<C, P, false, MODE><<<L->grid, kBlock, 0, L->stream>>>(L->a);
+            return after_launch("to_map (no-alloc)");
+        }
+    };
+    template <int C, int P>
     int run() {
-        k_scatter<C, P, false, SO3G_POINTING_EXACT><<<grid, kBlock, 0, stream>>>(a);
-        return after_launch("to_map (no-alloc)");
+        Go<C, P> g{this};
+        return by_mode<C, P>(a.fast, g);
     }
 };
 
@@ -118,11 +134,17 @@ extern "C" int so3g_proj_to_map_noalloc(
     int rc = scratch_address(&scr);
     if (rc) return rc;
 
-    NoAllocLaunch L;
+    NoAllocLaunch L{};
     rc = make_geom_lut(pz, &L.a.g, reinterpret_cast<const double *>(scr + kOffLut));
     if (rc) return rc;
+    const float4 *knots = reinterpret_cast<const float4 *>(scr + kOffKnots);
+    L.a.ft = FastTables{knots, knots + kLutN, knots + 2 * kLutN};
+    L.a.fast = fast_mode(pz, L.a.ft);
     if (!map_data) return set_error(SO3G_ERR_ARGUMENT, "map is NULL");
     cudaStream_t st = (cudaStream_t)stream;
+    rc = upload_tables(scr, L.a.fast != SO3G_POINTING_EXACT, st);
+    if (rc) return rc;
+    bool host_tables = false;
     if (pz->tiled) {
         if (!host_tile_offset)
             return set_error(SO3G_ERR_ARGUMENT, "tiled map needs a host tile_offset table");
@@ -135,6 +157,7 @@ extern "C" int so3g_proj_to_map_noalloc(
             return set_error(SO3G_ERR_CUDA, "tile table copy: %s", cudaGetErrorString(e));
         L.a.g.tile_offset = reinterpret_cast<const long long *>(scr + kOffTiles);
         L.a.g.n_tile_map = n_tile;
+        host_tables = true;
     }
     long long n_work = n_det, max_len = n_time;
     const int *dseg = nullptr;
@@ -153,6 +176,7 @@ extern "C" int so3g_proj_to_map_noalloc(
                                             cudaMemcpyHostToDevice, st);
             if (e != cudaSuccess)
                 return set_error(SO3G_ERR_CUDA, "segment copy: %s", cudaGetErrorString(e));
+            host_tables = true;
         }
         dseg = reinterpret_cast<const int *>(scr + kOffSegs);
     }
@@ -169,12 +193,13 @@ extern "C" int so3g_proj_to_map_noalloc(
         L.a.sig_stride = sig_det_stride;
         L.a.det_weights = det_weights;
         L.a.segs = Segs{dseg, n_time};
-        L.a.piece = piece_len(max_len);
+        L.a.piece = piece_len(max_len, n_work);
         L.a.accum = accum;
         L.a.err = derr;
         L.a.map = map_data;
-        L.a.fast = 0;  // exact pointing: the double-float knots are not in the scratch
-        L.a.bore32 = nullptr;
+        L.a.fc = make_fast_const(L.a.g);
+        L.a.mc = make_mixed_const(L.a.g);
+        L.a.bore32 = nullptr;   // the kernels round the float64 boresight themselves
         L.grid = dim3((unsigned)n_work, (unsigned)((max_len + L.a.piece - 1) / L.a.piece));
         L.stream = st;
         rc = dispatch_cp(pz->coord_sys, pix_kind(pz), L);
@@ -185,6 +210,26 @@ extern "C" int so3g_proj_to_map_noalloc(
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess)
             return set_error(SO3G_ERR_CUDA, "error record read: %s", cudaGetErrorString(e));
+    } else if (host_tables) {
+        // The caller may reuse host_seg / host_tile_offset on return.
+        e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess)
+            return set_error(SO3G_ERR_CUDA, "stream wait: %s", cudaGetErrorString(e));
     }
+    return SO3G_OK;
+}
+
+extern "C" int so3g_noalloc_read_error(int32_t *host_err, void *stream) {
+    clear_error();
+    if (!host_err) return set_error(SO3G_ERR_ARGUMENT, "host_err is NULL");
+    unsigned char *scr = nullptr;
+    int rc = scratch_address(&scr);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaMemcpyAsync(host_err, scr + kOffErr, 4 * sizeof(int),
+                                    cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess)
+        return set_error(SO3G_ERR_CUDA, "error record read: %s", cudaGetErrorString(e));
     return SO3G_OK;
 }

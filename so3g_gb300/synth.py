@@ -80,3 +80,53 @@ def native(proj, Q):
     """q_native = q_celestial_to_native * Q as a plain (n, 4) array."""
     return np.ascontiguousarray(np.asarray(proj.q_celestial_to_native *
                                            quat.G3VectorQuat(Q)), dtype=np.float64)
+
+
+# The benchmark workloads: focal plane radius (deg), scan (el, az throw and
+# speed in deg and deg/s, azimuth drift in deg/hour) and map of each.
+#   car  -- CAR TQU map of `shape` pixels at `res_arcmin`, centred on the scan
+#   hp   -- HEALPix TQU, RING untiled or NEST tiled (nside_tile)
+#   zea  -- ZEA bilinear TQU map, as car
+WORKLOADS = {
+    "cfg1": dict(kind="car", n_det=64, n_time=100_000, radius=1.0, shape=(600, 600),
+                 res_arcmin=1.0, el=50., throw=10., v_az=1., drift=0.),
+    "cfg2": dict(kind="car", n_det=1000, n_time=1_000_000, radius=1.5, shape=(2000, 2000),
+                 res_arcmin=1.0, el=50., throw=10., v_az=1., drift=0.),
+    "cfg3": dict(kind="hp", n_det=2000, n_time=2_000_000, radius=1.5, nside=1024,
+                 nside_tile=16, el=45., throw=30., v_az=2., drift=15.),
+    "cfg5": dict(kind="zea", n_det=4000, n_time=2_000_000, radius=1.5, shape=(3000, 3000),
+                 res_arcmin=0.5, el=50., throw=10., v_az=1., drift=0.),
+}
+
+
+def projection_inputs(c, seed=0, dets=None, tiled=False, tile_shape=(100, 100)):
+    """(projectionist, q_native (n_time, 4), dets (n_det, 4), resp (n_det, 2))
+    of a workload dict `c` (WORKLOADS entries, possibly with n_det/n_time
+    changed).  `dets` selects detectors of the full focal plane (e.g. every
+    20th, so a slice keeps the focal plane's footprint).  tiled: the NEST
+    tiled HEALPix map (nside_tile), or a flat map cut into tile_shape tiles
+    with every tile present."""
+    from .proj.wcs import ProjectionistHealpix
+    rng = np.random.default_rng(seed)
+    d, resp, _ = focal_plane(rng, c["n_det"], c["radius"])
+    if dets is not None:
+        d, resp = d[dets], resp[dets]
+    el = c.get("el", 50.)
+    Q, _ = scan(c["n_time"], rate=200., el=el, az0=180., throw=c.get("throw", 10.),
+                v_az=c.get("v_az", 1.), drift_deg_per_hour=c.get("drift", 0.))
+    kind = c.get("kind", "car")
+    if kind == "hp":
+        if tiled:
+            nt = 12 * c["nside_tile"] ** 2
+            p = ProjectionistHealpix.for_healpix(c["nside"], nside_tile=c["nside_tile"],
+                                                 active_tiles=list(range(nt)), ordering="NEST")
+        else:
+            p = ProjectionistHealpix.for_healpix(c["nside"], ordering="RING")
+    elif kind == "zea":
+        p = car_projectionist(c["shape"], c["res_arcmin"] * ARCMIN, el=el, az0=180.,
+                              proj="ZEA", interpol="bilinear")
+    else:
+        p = car_projectionist(c["shape"], c.get("res_arcmin", 1.) * ARCMIN, el=el, az0=180.,
+                              proj=c.get("proj", "CAR"),
+                              tile_shape=tile_shape if tiled else None)
+    return p, native(p, Q), np.ascontiguousarray(d), np.ascontiguousarray(resp)

@@ -82,3 +82,29 @@ def test_finite_differences():
     fd, g = np.array(errs).T
     assert np.any(g != 0)
     assert np.all(np.abs(fd - g) <= 1e-3 * np.maximum(1.0, np.abs(g)))
+
+
+def test_backward_uses_the_forward_pointing_mode():
+    """The pointing mode is pinned at forward: a caller that switches
+    eng.pointing before backward still gets to_map in the forward's mode
+    (mixed here), and its own setting back afterwards."""
+    import torch
+    from so3g_gb300 import _abi
+    eng, (q, dets, resp), m, d = _setup("CAR", "nearest")
+    eng.pointing = _abi.POINTING_MIXED
+    mm = m.clone().requires_grad_(True)
+    sig = autograd.from_map(eng, mm, q, dets, resp)
+    eng.pointing = _abi.POINTING_EXACT
+    (sig * d).sum().backward()
+    assert eng.pointing == _abi.POINTING_EXACT
+    eng.pointing = _abi.POINTING_MIXED
+    want = torch.zeros_like(m)
+    eng.to_map(want, q, dets, resp, d, None, None)
+    eng.pointing = _abi.POINTING_EXACT
+    exact = torch.zeros_like(m)
+    eng.to_map(exact, q, dets, resp, d, None, None)
+    scale = float(want.abs().max())
+    assert float((mm.grad - want).abs().max()) <= 1e-12 * scale
+    # The two modes' maps differ (float32 spin factors), so the check above
+    # does tell them apart.
+    assert float((exact - want).abs().max()) > 1e-12 * scale

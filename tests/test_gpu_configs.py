@@ -1,0 +1,338 @@
+"""Parity at the benchmark workloads' own geometry and scale, against the
+CPU oracle (the reference's ProjectionEngine arithmetic restated).
+
+- cfg1 in full: 64 detectors x 100,000 samples, CAR TQU 600 x 600 at 1'.
+- a cfg2 slice: every 20th detector of the 1000-detector focal plane
+  (50 detectors) x 1,000,000 samples, CAR TQU 2000 x 2000 at 1'.
+- a cfg3 slice: 20 detectors spread over the 2000-detector focal plane x
+  2,000,000 samples (4e7 samples), HEALPix nside 1024, RING untiled and
+  NEST tiled with nside_tile 16.
+- a cfg5 slice: 16 detectors spread over the 4000-detector focal plane x
+  500,000 samples, ZEA bilinear TQU 3000 x 3000 at 0.5'.
+
+Pixel indices are compared sample by sample in every pointing mode: the
+T-only engine of the same pixelization runs from_map of a map holding
+1 + each pixel's own index, which returns every sample's pixel index
+exactly (float32 holds integers below 2^24).  Mismatch counts must be 0.
+
+Maps are compared pixel by pixel, relative to each pixel's hit-weighted
+scale s_p = sum over the samples hitting p of |signal| * max(|T|, |P|)
+(the sum of the magnitudes of the terms added into p): exact and
+certified pointing to 1e-12 s_p (the float64 summation order), mixed
+pointing to MIXED_PF_BOUND s_p, the bound on a float32 spin factor's
+error, and to 1e-6 of the map's largest |value|.  Signals from from_map are
+compared sample by sample against the per-sample scale sum_c |m_c[p]| *
+max(|T|, |P|): bit for bit for exact and certified nearest-neighbour
+pointing, within the same bounds otherwise.
+"""
+import numpy as np
+import pytest
+
+from so3g_gb300 import _abi, synth
+
+pytestmark = pytest.mark.gpu
+
+MODES = {"exact": _abi.POINTING_EXACT, "certified": _abi.POINTING_CERTIFIED,
+         "mixed": _abi.POINTING_MIXED}
+# Error bound of a float32 spin factor of the mixed pointing, relative to
+# the response P: the float32 boresight and detector quaternions and the
+# product's roundings (|dq| <= 10u, u = 2^-24) turn the polarisation angle
+# by <= 4|dq| / cos(lat) and the float32 evaluation of (Nc^2 - Ns^2)/D and
+# 2 Nc Ns / D adds a few u; cos(lat) >= 0.44 inside the float32 tier's
+# |sin lat| < 0.9 guard.  The samples the float32 tier leaves get the
+# nearest floats from the double-float path.
+MIXED_PF_BOUND = 2e-5
+RTOL_EXACT = 1e-12
+RTOL_GLOBAL_MIXED = 1e-6
+
+
+def _workload(name, n_det=None, n_time=None, every=None, tiled=False):
+    c = dict(synth.WORKLOADS[name])
+    full = c["n_det"]
+    dets = None
+    if every is not None:
+        dets = np.arange(0, full, every)[:n_det]
+    elif n_det is not None:
+        c["n_det"] = n_det
+    if n_time is not None:
+        c["n_time"] = n_time
+    p, q, d, resp = synth.projection_inputs(c, dets=dets, tiled=tiled)
+    return c, p, q, d, resp
+
+
+def _signal(n_det, n_time, seed=0):
+    rng = np.random.default_rng(seed)
+    return rng.standard_normal((n_det, n_time), dtype=np.float32)
+
+
+def _pz(eng, mode=None, ncomp=None):
+    pz = eng._pz()
+    if mode is not None:
+        pz.pointing = mode
+    if ncomp is not None:
+        pz.n_comp = ncomp
+    return pz
+
+
+# -- pixel indices -----------------------------------------------------------
+
+def _flat_index(pix, nx):
+    """Oracle pixels (..., 2) of an untiled flat map -> parent index, -1 off."""
+    return np.where(pix[..., 0] >= 0, pix[..., 0].astype(np.int64) * nx + pix[..., 1], -1)
+
+
+def _probe_map(eng, kind):
+    """T-only map holding 1 + the pixel's own index (HEALPix: the index in
+    the map's ordering; tiled HEALPix: the NEST index)."""
+    if kind == "flat":
+        ny, nx = eng.naxis
+        return (1. + np.arange(ny * nx, dtype=np.float64)).reshape(1, ny, nx)
+    if kind == "hp":
+        return (1. + np.arange(12 * eng.nside ** 2, dtype=np.float64)).reshape(1, -1)
+    nppt = 12 * eng.nside ** 2 // eng._n_tile()
+    return [(1. + i * nppt + np.arange(nppt, dtype=np.float64)).reshape(1, -1)
+            for i in range(eng._n_tile())]
+
+
+def _probe_pixels(p, q, d, mode, kind):
+    """Every sample's pixel index from the GPU in pointing mode `mode`
+    (-1 off the map)."""
+    import torch
+    eng = p.get_ProjEng("T")
+    eng.pointing = mode
+    m = _probe_map(eng, kind)
+    dev = torch.device("cuda", 0)
+    if isinstance(m, list):
+        m = [torch.from_numpy(t).to(dev) for t in m]
+    else:
+        m = torch.from_numpy(m).to(dev)
+    ones = torch.ones((len(d), 2), dtype=torch.float32, device=dev)
+    out = eng.from_map(m, torch.from_numpy(q).to(dev), torch.from_numpy(d).to(dev), ones, None)
+    return out.cpu().numpy().astype(np.int64) - 1
+
+
+# -- maps ----------------------------------------------------------------------
+
+def _hit_scale(orc, eng, q, d, resp, sig, ncomp, weight=False):
+    """Per-pixel sum of the magnitudes of the terms (flat (npix,) array)."""
+    amp = np.max(np.abs(resp), axis=1)
+    r = np.stack([amp, amp], axis=1).astype(np.float32)
+    pzT = _pz(eng, _abi.POINTING_EXACT, 1)
+    s = np.zeros(int(np.prod(eng._pix_shape())))
+    if weight:
+        # T-only weights: sum of T^2 = max(|T|, |P|)^2 >= |pf_i pf_j|.
+        orc.to_weight_map(pzT, q, d, r, None, s)
+    else:
+        orc.to_map(pzT, q, d, r, np.abs(sig), None, s)
+    return s
+
+
+def _check_map(got, want, scale, ncomp, rtol, what):
+    got = np.asarray(got).reshape(ncomp, -1)
+    want = want.reshape(ncomp, -1)
+    err = np.abs(got - want)
+    rel = (err / np.maximum(scale, 1e-300)[None, :]).max()
+    big = np.abs(want).max()
+    assert np.all(err <= rtol * scale[None, :] + 1e-300), (what, rel)
+    return rel, err.max() / big
+
+
+def _to_map_case(orc, p, q, d, resp, sig, mode, rtol):
+    import torch
+    eng = p.get_ProjEng("TQU")
+    eng.pointing = mode
+    shape = (3,) + tuple(eng._pix_shape())
+    dev = torch.device("cuda", 0)
+    got = torch.zeros(shape, dtype=torch.float64, device=dev)
+    eng.to_map(got, torch.from_numpy(q).to(dev), torch.from_numpy(d).to(dev),
+               torch.from_numpy(resp).to(dev), torch.from_numpy(sig).to(dev), None, None)
+    got = got.cpu().numpy()
+    want = np.zeros(int(np.prod(shape)))
+    orc.to_map(_pz(eng, _abi.POINTING_EXACT), q, d, resp, sig, None, want)
+    scale = _hit_scale(orc, eng, q, d, resp, sig, 3)
+    rel, glob = _check_map(got, want, scale, 3, rtol, "to_map")
+    return eng, want, rel, glob
+
+
+def _from_map_case(orc, eng, q, d, resp, m, mode, exact_bits):
+    import torch
+    eng.pointing = mode
+    dev = torch.device("cuda", 0)
+    got = eng.from_map(torch.from_numpy(m).to(dev), torch.from_numpy(q).to(dev),
+                       torch.from_numpy(d).to(dev), torch.from_numpy(resp).to(dev),
+                       None).cpu().numpy()
+    want = np.zeros(got.shape, np.float32)
+    orc.from_map(_pz(eng, _abi.POINTING_EXACT), q, d, resp, m.ravel().copy(), want)
+    if exact_bits:
+        n_bad = int(np.count_nonzero(got.view(np.int32) != want.view(np.int32)))
+        assert n_bad == 0, n_bad
+        return 0.
+    # Per-sample scale: sum_c |m_c[p]| * max(|T|, |P|) (bilinear: the taps'
+    # weights sum to <= 1, so the largest tap's scale bounds it).
+    amp = np.max(np.abs(resp), axis=1)
+    mabs = np.abs(m).sum(axis=0).reshape(1, *m.shape[1:])
+    pzT = _pz(eng, _abi.POINTING_EXACT, 1)
+    sc = np.zeros(got.shape, np.float32)
+    orc.from_map(pzT, q, d, np.stack([amp, amp], 1).astype(np.float32), mabs.ravel().copy(),
+                 sc)
+    rel = np.abs(got.astype(np.float64) - want) / np.maximum(sc.astype(np.float64), 1e-30)
+    return float(rel.max())
+
+
+# -- cfg1: the whole workload ------------------------------------------------------
+
+@pytest.fixture(scope="module")
+def cfg1():
+    c, p, q, d, resp = _workload("cfg1")
+    return p, q, d, resp, _signal(c["n_det"], c["n_time"])
+
+
+def test_cfg1_pixels_every_mode(orc, gpulib, cfg1):
+    p, q, d, resp, sig = cfg1
+    eng = p.get_ProjEng("TQU")
+    want = _flat_index(orc.pixels(_pz(eng, _abi.POINTING_EXACT), q, d, 2), eng.naxis[1])
+    on = want >= 0
+    # The 600' map is narrower than the ~13' wide scan: part of the samples
+    # fall off it.
+    print("cfg1 hit fraction %.4f of %d samples" % (on.mean(), want.size))
+    assert 0.3 < on.mean() < 0.99
+    for name, mode in MODES.items():
+        got = _probe_pixels(p, q, d, mode, "flat")
+        n_bad = int(np.count_nonzero(got != want))
+        print("cfg1 %s: pixel mismatches %d of %d" % (name, n_bad, want.size))
+        assert n_bad == 0, (name, n_bad)
+
+
+@pytest.mark.parametrize("name", list(MODES))
+def test_cfg1_to_map_per_pixel(orc, gpulib, cfg1, name):
+    p, q, d, resp, sig = cfg1
+    mode = MODES[name]
+    rtol = MIXED_PF_BOUND if name == "mixed" else RTOL_EXACT
+    eng, want, rel, glob = _to_map_case(orc, p, q, d, resp, sig, mode, rtol)
+    print("cfg1 %s to_map: max error / hit scale %.2e, / max|map| %.2e" % (name, rel, glob))
+    if name == "mixed":
+        assert glob <= RTOL_GLOBAL_MIXED
+    # from_map of the oracle's map.
+    m = want.reshape((3,) + tuple(eng._pix_shape()))
+    r = _from_map_case(orc, eng, q, d, resp, m, mode, exact_bits=name != "mixed")
+    print("cfg1 %s from_map: max error / sample scale %.2e" % (name, r))
+    assert r <= MIXED_PF_BOUND
+
+
+@pytest.mark.parametrize("name", list(MODES))
+def test_cfg1_to_weight_map_per_pixel(orc, gpulib, cfg1, name):
+    import torch
+    p, q, d, resp, sig = cfg1
+    mode = MODES[name]
+    eng = p.get_ProjEng("TQU")
+    eng.pointing = mode
+    shape = (3, 3) + tuple(eng._pix_shape())
+    dev = torch.device("cuda", 0)
+    got = torch.zeros(shape, dtype=torch.float64, device=dev)
+    eng.to_weight_map(got, torch.from_numpy(q).to(dev), torch.from_numpy(d).to(dev),
+                      torch.from_numpy(resp).to(dev), None, None)
+    want = np.zeros(int(np.prod(shape)))
+    orc.to_weight_map(_pz(eng, _abi.POINTING_EXACT), q, d, resp, None, want)
+    scale = _hit_scale(orc, eng, q, d, resp, sig, 3, weight=True)
+    # Products of two spin factors: twice the single-factor bound.
+    rtol = 2 * MIXED_PF_BOUND if name == "mixed" else RTOL_EXACT
+    rel, glob = _check_map(got.cpu().numpy(), want, scale, 9, rtol, "to_weight_map")
+    print("cfg1 %s to_weight_map: max error / hit scale %.2e, / max|map| %.2e" %
+          (name, rel, glob))
+
+
+# -- cfg2: every 20th detector, every sample ------------------------------------
+
+@pytest.mark.parametrize("name", ["certified", "mixed"])
+def test_cfg2_slice(orc, gpulib, name):
+    c, p, q, d, resp = _workload("cfg2", n_det=50, every=20)
+    sig = _signal(len(d), c["n_time"], seed=2)
+    mode = MODES[name]
+    eng = p.get_ProjEng("TQU")
+    want = _flat_index(orc.pixels(_pz(eng, _abi.POINTING_EXACT), q, d, 2), eng.naxis[1])
+    got = _probe_pixels(p, q, d, mode, "flat")
+    n_bad = int(np.count_nonzero(got != want))
+    print("cfg2 slice %s: pixel mismatches %d of %d" % (name, n_bad, want.size))
+    assert n_bad == 0
+    del got, want
+    rtol = MIXED_PF_BOUND if name == "mixed" else RTOL_EXACT
+    eng, want, rel, glob = _to_map_case(orc, p, q, d, resp, sig, mode, rtol)
+    print("cfg2 slice %s to_map: max error / hit scale %.2e, / max|map| %.2e" %
+          (name, rel, glob))
+    if name == "mixed":
+        assert glob <= RTOL_GLOBAL_MIXED
+    m = want.reshape((3,) + tuple(eng._pix_shape()))
+    r = _from_map_case(orc, eng, q, d, resp, m, mode, exact_bits=name != "mixed")
+    print("cfg2 slice %s from_map: max error / sample scale %.2e" % (name, r))
+    assert r <= MIXED_PF_BOUND
+
+
+# -- cfg3: HEALPix nside 1024, 4e7 samples -----------------------------------------
+
+@pytest.mark.parametrize("tiled", [False, True])
+def test_cfg3_slice_coords_and_pixels(orc, gpulib, tiled):
+    import torch
+    c, p, q, d, resp = _workload("cfg3", n_det=20, every=100, tiled=tiled)
+    eng = p.get_ProjEng("TQU")
+    pz = _pz(eng, _abi.POINTING_EXACT)
+    dev = torch.device("cuda", 0)
+    qd = torch.from_numpy(q).to(dev)
+    n_coord_bad = n_pix_bad = 0
+    want_all = []
+    for a in range(0, len(d), 5):
+        dd = np.ascontiguousarray(d[a:a + 5])
+        got = eng.coords(qd, torch.from_numpy(dd).to(dev), None).cpu().numpy()
+        want = orc.coords(pz, q, dd)
+        n_coord_bad += int(np.count_nonzero(np.any(got.view(np.int64) != want.view(np.int64),
+                                                   axis=-1)))
+        del got, want
+        gp = np.asarray(eng.pixels(qd, torch.from_numpy(dd).to(dev), None).cpu().numpy())
+        wp = orc.pixels(pz, q, dd, eng.index_count)
+        n_pix_bad += int(np.count_nonzero(np.any(gp != wp, axis=-1)))
+        want_all.append(wp[..., 0] if not tiled else
+                        wp[..., 0].astype(np.int64) * (12 * eng.nside ** 2 // eng._n_tile()) +
+                        wp[..., 1])
+        del gp, wp
+    n = len(d) * c["n_time"]
+    print("cfg3 slice %s: coords mismatches %d, pixel mismatches %d of %d samples" %
+          ("tiled NEST" if tiled else "RING", n_coord_bad, n_pix_bad, n))
+    assert n_coord_bad == 0 and n_pix_bad == 0
+    want = np.concatenate(want_all).astype(np.int64)
+    for name in ("certified", "mixed"):
+        got = _probe_pixels(p, q, d, MODES[name], "hp_tiled" if tiled else "hp")
+        n_bad = int(np.count_nonzero(got != want))
+        print("cfg3 slice %s %s: pixel mismatches %d of %d" %
+              ("tiled NEST" if tiled else "RING", name, n_bad, n))
+        assert n_bad == 0
+
+
+def test_cfg3_slice_maps(orc, gpulib):
+    """to_map of the RING map in the mixed mode (the bench's) on 4e6 samples."""
+    c, p, q, d, resp = _workload("cfg3", n_det=4, every=500, n_time=1_000_000)
+    sig = _signal(len(d), c["n_time"], seed=3)
+    for name in ("certified", "mixed"):
+        rtol = MIXED_PF_BOUND if name == "mixed" else RTOL_EXACT
+        eng, want, rel, glob = _to_map_case(orc, p, q, d, resp, sig, MODES[name], rtol)
+        print("cfg3 slice %s to_map: max error / hit scale %.2e, / max|map| %.2e" %
+              (name, rel, glob))
+
+
+# -- cfg5: ZEA bilinear ------------------------------------------------------------
+
+def test_cfg5_slice(orc, gpulib):
+    c, p, q, d, resp = _workload("cfg5", n_det=16, every=250, n_time=500_000)
+    sig = _signal(len(d), c["n_time"], seed=5)
+    eng = p.get_ProjEng("TQU")
+    rng = np.random.default_rng(9)
+    field = rng.standard_normal((3,) + tuple(eng._pix_shape()))
+    for name in MODES:
+        mode = MODES[name]
+        # Certified bilinear weights are within one float32 ulp of the
+        # reference's; mixed bilinear keeps the double-float taps with
+        # float32 spin factors and terms.
+        rtol = RTOL_EXACT if name == "exact" else 1e-6
+        e, want, rel, glob = _to_map_case(orc, p, q, d, resp, sig, mode, rtol)
+        r = _from_map_case(orc, e, q, d, resp, field, mode, exact_bits=name == "exact")
+        print("cfg5 slice %s: to_map error / hit scale %.2e; from_map error / sample "
+              "scale %.2e" % (name, rel, r))
+        assert r <= 1e-6

@@ -23,7 +23,14 @@ def test_coords(orc, gpulib, coord):
     if coord in EXACT:
         assert bits_equal(got, want)
     else:
-        np.testing.assert_allclose(got, want, rtol=4e-16, atol=1e-15)
+        # CEA: the longitude is the math library's atan2 -- CUDA's and the
+        # host's may round differently in the last bit.  Counted; every
+        # other coordinate must be bit-identical.
+        diff = got.view(np.int64) != want.view(np.int64)
+        n_lon = int(np.count_nonzero(diff[..., 0]))
+        print("CEA coords: %d of %d longitudes differ in the last bit" % (n_lon, diff[..., 0].size))
+        assert not diff[..., 1:].any()
+        np.testing.assert_allclose(got[..., 0], want[..., 0], rtol=4e-16, atol=1e-15)
 
 
 @pytest.mark.parametrize("coord", COORDS)
@@ -36,13 +43,14 @@ def test_pixels(orc, gpulib, coord, tiled):
     # Some samples are off the map, so the carried ("stale") slots are
     # exercised too.
     assert (want[..., 0] == -1).any() and (want[..., 0] >= 0).any()
-    if coord in EXACT:
-        assert np.array_equal(got, want)
-    else:
-        assert np.mean(np.any(got != want, axis=-1)) < 1e-3
+    # CEA's last-bit atan2 differences move a pixel only for a sample within
+    # ~1e-16 of a pixel edge: the count must be 0 here as for the others.
+    n_bad = int(np.count_nonzero(np.any(got != want, axis=-1)))
+    print("%s pixels: %d of %d samples differ" % (coord, n_bad, got.shape[0] * got.shape[1]))
+    assert n_bad == 0
 
 
-@pytest.mark.parametrize("coord", ["CAR", "TAN", "ZEA", "ARC", "SIN", "Flat"])
+@pytest.mark.parametrize("coord", COORDS)
 @pytest.mark.parametrize("ncomp", [1, 2, 3])
 @pytest.mark.parametrize("tiled", [False, True])
 def test_pointing_matrix(orc, gpulib, coord, ncomp, tiled):

@@ -1,7 +1,11 @@
 """Projection parity on the GPU: to_map, to_weight_map and from_map of the
 CUDA library against the CPU oracle on the same seeded inputs.
 
-Both pointing modes are checked.  Tolerances: from_map evaluates each
+Every pointing mode is checked, for every coordinate system.  CEA's
+longitude comes from the math library's atan2 (src/Projection.cxx:468),
+whose CUDA and host roundings may differ in the last bit; that moves a
+pixel index only for a sample within ~1e-16 of a pixel edge, which these
+inputs do not have, so CEA is held to the same bounds.  Tolerances: from_map evaluates each
 sample exactly as the reference does and is compared bit for bit.
 to_map/to_weight_map form every float32 term exactly as the reference does;
 only the order of the float64 sums differs (atomics, and the warp
@@ -59,7 +63,8 @@ def oracle_to_weight(orc, c, m, det_weights=None, threads=None):
     return map_from_oracle(flat, offs, m), err
 
 
-CASES = [(coord, tiled, bil) for coord in ["CAR", "TAN", "ZEA", "ARC", "SIN", "Flat", "Quat"]
+CASES = [(coord, tiled, bil)
+         for coord in ["CAR", "CEA", "TAN", "ZEA", "ARC", "SIN", "Flat", "Quat"]
          for tiled in (False, True) for bil in (False, True)]
 
 

@@ -6,9 +6,11 @@ Called through the C ABI, it must give the maps of so3g_proj_to_map within
 the to_map tolerance of the other tests (1e-12 of the map's scale), on two
 calls in a row -- the second with different tiles and segments, so nothing
 of the first call's scratch may leak into it -- and must clear the error
-record at each call.  This file is collected last so that a run stopping
-at the first failure has run every other test first; it also passes alone
-in a fresh process."""
+record at each call.  It is also compared with the CPU oracle in every
+pointing mode for a CAR, a TAN and a tiled HEALPix (NEST) map, and its
+error record is read back after a call made without host_err.  This file
+is collected last so that a run stopping at the first failure has run
+every other test first; it also passes alone in a fresh process."""
 import ctypes
 
 import numpy as np
@@ -167,3 +169,93 @@ def test_noalloc_rejects_oversize():
                                       _abi.ACCUM_ATOMIC, None, None)
     assert rc == -4
     assert "at most 65536 sample segments" in _abi.last_error()
+
+
+def _noalloc_case(lib, c, mode, seg=None):
+    """so3g_proj_to_map_noalloc of a helpers.Case in pointing mode `mode`;
+    returns the flat map and its tile offsets (None if untiled)."""
+    import torch
+    from so3g_gb300 import _abi
+    from helpers import oracle_map
+    dev = torch.device("cuda", torch.cuda.current_device())
+    flat, offs = oracle_map(c.blank((c.ncomp,)))
+    m = torch.zeros(flat.size, dtype=torch.float64, device=dev)
+    q, d, r, s = (torch.from_numpy(np.ascontiguousarray(x)).to(dev)
+                  for x in (c.bore, c.dets, c.resp, c.signal))
+    pz = c.eng._pz()
+    pz.pointing = mode
+    host_err = np.full(4, -7, dtype=np.int32)
+    rc = lib.so3g_proj_to_map_noalloc(
+        pz, q.data_ptr(), c.n_time, d.data_ptr(), c.n_det, r.data_ptr(), s.data_ptr(),
+        c.n_time, None, None if seg is None else seg.ctypes.data,
+        0 if seg is None else len(seg), m.data_ptr(),
+        None if offs is None else offs.ctypes.data, 0 if offs is None else len(offs),
+        _abi.ACCUM_WARP_RUNS, host_err.ctypes.data, torch.cuda.current_stream().cuda_stream)
+    assert rc == 0, _abi.last_error()
+    assert np.all(host_err == 0)
+    return m.cpu().numpy(), offs
+
+
+@pytest.mark.parametrize("kind", ["CAR", "TAN", "HP_NEST_TILED"])
+def test_noalloc_every_pointing_mode_against_oracle(orc, kind):
+    """Each pointing mode twice in a row against the oracle (exact and
+    certified: 1e-12 of the map's scale, the float64 summation order; mixed:
+    float32 spin factors, 1e-6 of the scale) and against so3g_proj_to_map
+    in the same mode (1e-12)."""
+    from so3g_gb300 import _abi
+    from helpers import Case, oracle_map
+    lib = _abi.lib()
+    assert lib.so3g_init() == 0
+    if kind == "HP_NEST_TILED":
+        c = Case(orc, coord="CAR", hp=(256, True, 8), tiled=True, n_det=6, n_time=6000,
+                 seed=21)
+        hits = np.array(c.eng.tile_hits(c.bore, c.dets))
+        c = Case(orc, coord="CAR", hp=(256, True, 8), tiled=True, n_det=6, n_time=6000,
+                 seed=21, active=[int(i) for i in np.nonzero(hits)[0]])
+    else:
+        c = Case(orc, coord=kind, n_det=6, n_time=6000, seed=22)
+    want, woffs = oracle_map(c.blank((c.ncomp,)))
+    orc.to_map(c.pz, c.bore, c.dets, c.resp, c.signal, None, want, woffs)
+    scale = np.abs(want).max()
+    assert scale > 0
+    for mode, tol in ((_abi.POINTING_EXACT, 1e-12), (_abi.POINTING_CERTIFIED, 1e-12),
+                      (_abi.POINTING_MIXED, 1e-6)):
+        for _ in range(2):
+            got, offs = _noalloc_case(lib, c, mode)
+            assert offs is None or np.array_equal(offs, woffs)
+            assert np.abs(got - want).max() <= tol * scale, (mode, np.abs(got - want).max())
+        c.eng.pointing = mode
+        ref = c.eng.to_map(None, c.bore, c.dets, c.resp, c.signal, None, None)
+        from helpers import stack_map
+        assert np.abs(got - stack_map(ref)).max() <= 1e-12 * scale, mode
+
+
+def test_noalloc_read_error_after_call_without_host_err():
+    """A call onto an absent tile made with host_err = NULL leaves the
+    record for so3g_noalloc_read_error; the next call clears it."""
+    import torch
+    from so3g_gb300 import _abi
+    lib = _abi.lib()
+    eng, t, nd, nt = _inputs(6, tiled=True)
+    hits = np.array(eng.tile_hits(t["q"], t["d"]))
+    hit = np.nonzero(hits)[0]
+    offs, size = _tile_layout(eng, set(range(eng._n_tile())) - {int(hit[-1])})
+    m = torch.zeros(max(size, 1), dtype=torch.float64, device=t["q"].device)
+    stream = torch.cuda.current_stream().cuda_stream
+    for want_err in (True, False):
+        o = offs if want_err else _tile_layout(eng, set(range(eng._n_tile())))[0]
+        if not want_err:
+            m = torch.zeros(_tile_layout(eng, set(range(eng._n_tile())))[1],
+                            dtype=torch.float64, device=t["q"].device)
+        rc = lib.so3g_proj_to_map_noalloc(
+            eng._pz(), t["q"].data_ptr(), nt, t["d"].data_ptr(), nd, t["r"].data_ptr(),
+            t["s"].data_ptr(), nt, None, None, 0, m.data_ptr(), o.ctypes.data, len(o),
+            _abi.ACCUM_ATOMIC, None, stream)
+        assert rc == 0, _abi.last_error()
+        rec = np.full(4, -7, dtype=np.int32)
+        assert lib.so3g_noalloc_read_error(rec.ctypes.data, stream) == 0
+        if want_err:
+            assert rec[0] == _abi.DEVERR_MISSING_TILE and 2**31 - 1 - rec[1] == hit[-1]
+        else:
+            assert np.all(rec == 0)
+    assert lib.so3g_noalloc_read_error(None, stream) == -1
