@@ -13,6 +13,7 @@
 // exact path's.
 
 #include "host.h"
+#include "mx_common.cuh"
 
 namespace so3g {
 
@@ -465,6 +466,92 @@ __global__ void __launch_bounds__(kBlock, MixedEligible<C, P>::value && MODE == 
     }
 }
 
+// The two-pass mixed from_map of untiled nearest-neighbour maps (see
+// mx_common.cuh).  Main pass: the float32 tier on every sample, the map
+// read from its float32 copy (one 16-byte load), the signal updated where
+// the sample is certified and on the map; the samples it cannot certify
+// are left untouched and marked in the mask.
+template <int C, int P>
+__global__ void __launch_bounds__(kBlock, kMxBlocksPerSM) k_from_map_mx(GatherArgs a, MxMask mm) {
+    int det, t0, t1;
+    if (!seg_piece(a.segs, a.piece, det, t0, t1)) return;
+    const double *dq = a.dets + 4LL * det;
+    const float qd[4] = {d2f_round(__ldg(dq)), d2f_round(__ldg(dq + 1)), d2f_round(__ldg(dq + 2)),
+                         d2f_round(__ldg(dq + 3))};
+    const float T = __ldg(a.resp + 2 * det), Pr = __ldg(a.resp + 2 * det + 1);
+    const int nc = a.g.ncomp;
+    float *sig = a.signal + det * a.sig_stride;
+    unsigned *mw = mm.words + ((long long)blockIdx.x * gridDim.y + blockIdx.y) * mm.wpp +
+                   (threadIdx.x >> 5);
+    const int rounds = (t1 - t0 + kBlock - 1) / kBlock;
+    for (int r = 0; r < rounds; r++) {
+        const int t = t0 + r * kBlock + threadIdx.x;
+        const bool live = t < t1;
+        // Loaded before the pointing, so that its latency overlaps it.
+        const float s_in = live ? sig[t] : 0.f;
+        float qb[4] = {1.f, 0.f, 0.f, 0.f};
+        if (live) {
+            const float4 b = __ldg(a.bore32 + t);
+            qb[0] = b.x;
+            qb[1] = b.y;
+            qb[2] = b.z;
+            qb[3] = b.w;
+        }
+        int pix[2] = {0, 0};
+        float pf[3] = {0.f, 0.f, 0.f};
+        bool on = false;
+        const bool ok = live && mixed_pointing<C, P, true, false>(a.g, a.ft, a.mc, qb, qd, nc, T,
+                                                                  Pr, pix, on, pf);
+        const unsigned fails = __ballot_sync(kFull, live && !ok);
+        if (fails && (threadIdx.x & 31) == 0) mw[r * (kBlock / 32)] = fails;
+        if (ok && on) {
+            const int key = P == PX_HP_NT ? pix[0] : pix[0] * a.g.nx + pix[1];
+            const float4 m = __ldg(a.map32 + key);
+            // float32 terms (the mixed-precision contract).
+            float s = fmaf(m.x, pf[0], s_in);
+            if (nc > 1) s = fmaf(m.y, pf[1], s);
+            if (nc > 2) s = fmaf(m.z, pf[2], s);
+            sig[t] = s;
+        }
+    }
+}
+
+// Fallback pass of k_from_map_mx: double-float pointing (float32 spin
+// factors and terms), then the exact float64 pointing.
+template <int C, int P>
+__global__ void __launch_bounds__(kBlock) k_from_map_mx_fix(GatherArgs a, MxMask mm) {
+    mx_for_each(a.segs, a.piece, mm, [&](int det, int t) {
+        const QuatD ofs = load_quat(a.dets + 4LL * det);
+        const dfl qd[4] = {df_of(ofs.a), df_of(ofs.b), df_of(ofs.c), df_of(ofs.d)};
+        const float T = __ldg(a.resp + 2 * det), Pr = __ldg(a.resp + 2 * det + 1);
+        if (!df_gather<C, P>(a, det, t, qd, T, Pr)) exact_gather<C, P>(a, det, t, ofs, T, Pr);
+    });
+}
+
+// Runs the two passes; returns 1 (nothing launched: the caller runs
+// k_from_map) when the pixelization is not eligible, the map has 2^31
+// pixels or more, a float32 copy is missing, or the mask cannot be
+// allocated.
+template <int C, int P>
+int gather_mixed(const GatherArgs &a, dim3 grid, cudaStream_t stream) {
+    if constexpr (!MxEligible<C, P>::value) {
+        return 1;
+    } else {
+        const long long npix = P == PX_HP_NT ? a.g.npix : (long long)a.g.ny * a.g.nx;
+        if (!a.bore32 || !a.map32 || npix >= (1LL << 31)) return 1;
+        MxMask mm;
+        if (!mx_mask_alloc(mm, grid, a.piece, stream)) return 1;
+        k_from_map_mx<C, P><<<grid, kBlock, 0, stream>>>(a, mm);
+        int rc = after_launch("from_map (mixed)");
+        if (rc == SO3G_OK) {
+            k_from_map_mx_fix<C, P><<<mx_fix_blocks(mm), kBlock, 0, stream>>>(a, mm);
+            rc = after_launch("from_map (mixed fallback)");
+        }
+        cudaFreeAsync(mm.words, stream);
+        return rc;
+    }
+}
+
 struct GatherLaunch {
     GatherArgs a;
     dim3 grid;
@@ -474,6 +561,10 @@ struct GatherLaunch {
         GatherLaunch *L;
         template <int MODE>
         int go() {
+            if constexpr (MODE == SO3G_POINTING_MIXED) {
+                const int rc = gather_mixed<C, P>(L->a, L->grid, L->stream);
+                if (rc != 1) return rc;
+            }
             k_from_map<C, P, MODE><<<L->grid, kBlock, 0, L->stream>>>(L->a);
             return after_launch("from_map");
         }

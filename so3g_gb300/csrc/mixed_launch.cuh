@@ -1,0 +1,183 @@
+// mixed_launch.cuh -- the streamlined to_map / to_weight_map of the mixed
+// pointing (SO3G_POINTING_MIXED) for untiled nearest-neighbour maps: CAR,
+// TAN, ZEA and SIN flat maps and HEALPix.
+//
+// Two kernels per call instead of one:
+//
+// - k_scatter_mx runs the float32 tier of mixedpoint.cuh on every sample
+//   (one sample per lane, a detector piece per block, as k_scatter) and
+//   accumulates what it certifies.  It keeps no fallback work of its own:
+//   each warp records the samples it could not certify as one 32-bit word
+//   per round (bit b = lane b) in a mask in global memory.  The loop body is
+//   then only the float32 pointing, its certificate, the products and the
+//   accumulation, with 32-bit pixel keys -- no per-warp queues, no inlined
+//   double-float or float64 code.
+// - k_scatter_mx_fix reads the mask warp by warp (32 words = 1024 samples
+//   at a time), hands the set bits out to the lanes by prefix sum so that
+//   every lane works on a sample, and sends each through the double-float
+//   pointing (float32 spin factors: the mixed contract) and, where that
+//   cannot certify the pixel either, the exact float64 pointing.
+//
+// The map is the same as k_scatter's up to the float64 summation order.
+#pragma once
+
+#include "mx_common.cuh"
+#include "scatter_kernel.cuh"
+
+namespace so3g {
+
+namespace {
+
+// flush_runs (device.cuh) with a 32-bit pixel key (-1: nothing to add):
+// runs of equal keys across the warp are summed in compensated float32 and
+// flushed with one float64 atomic per run and value; a warp with at least
+// DIRECT_RUNS runs adds every term with its own atomic.
+template <int NV>
+__device__ __forceinline__ void flush_runs32(int key, long long plane, float (&v)[NV],
+                                             const int (&mult)[NV], unsigned vmask,
+                                             double *map) {
+    const int lane = threadIdx.x & 31;
+    const int prev = __shfl_up_sync(kFull, key, 1);
+    const bool head = (lane == 0) || (key != prev);
+    const unsigned heads = __ballot_sync(kFull, head);
+    if (__popc(heads) >= kDirectRuns) {
+        if (key >= 0) {
+            double *p = map + key;
+#pragma unroll
+            for (int k = 0; k < NV; k++)
+                if ((vmask >> k) & 1u) atomicAdd(p + mult[k] * plane, f2d(v[k]));
+        }
+        return;
+    }
+    const unsigned after = heads & ~((2u << lane) - 1u);
+    const int end = after ? (__ffs(after) - 1) : 32;
+    const int span = head ? end - lane : 1;
+    const int maxrun = __reduce_max_sync(kFull, (unsigned)span);
+    float e[NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++) e[k] = 0.f;
+    for (int d = 1; d < maxrun; d <<= 1) {
+        const bool take = lane + d < end;
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            if (!((vmask >> k) & 1u)) continue;
+            const float os = __shfl_down_sync(kFull, v[k], d);
+            const float oe = __shfl_down_sync(kFull, e[k], d);
+            if (take) {
+                float s, r;
+                two_sum(v[k], os, s, r);
+                v[k] = s;
+                e[k] += oe + r;
+            }
+        }
+    }
+    if (head && key >= 0) {
+        double *p = map + key;
+#pragma unroll
+        for (int k = 0; k < NV; k++)
+            if ((vmask >> k) & 1u) atomicAdd(p + mult[k] * plane, f2d(v[k]) + f2d(e[k]));
+    }
+}
+
+// The main pass.  Block (x, y): piece y of segment x, in rounds of kBlock
+// samples (lane = sample).  Needs the float32 boresight copy (a.bore32).
+template <int C, int P, bool WEIGHT>
+__global__ void __launch_bounds__(kBlock, kMxBlocksPerSM) k_scatter_mx(ScatterArgs a, MxMask mm) {
+    int det, t0, t1;
+    if (!seg_piece(a.segs, a.piece, det, t0, t1)) return;
+    float det_wt = 1.f;
+    if (a.det_weights) {
+        det_wt = __ldg(a.det_weights + det);
+        if (det_wt == 0.f) return;  // src/Projection.cxx:1784-1788
+    }
+    const double *dq = a.dets + 4LL * det;
+    const float qd[4] = {d2f_round(__ldg(dq)), d2f_round(__ldg(dq + 1)), d2f_round(__ldg(dq + 2)),
+                         d2f_round(__ldg(dq + 3))};
+    const float T = __ldg(a.resp + 2 * det), Pr = __ldg(a.resp + 2 * det + 1);
+    const int nc = a.g.ncomp;
+    constexpr int NV = WEIGHT ? 6 : 3;
+    int mult[NV];
+    const unsigned vmask = value_slots<WEIGHT>(nc, mult);
+    const long long plane = P == PX_HP_NT ? a.g.npix : (long long)a.g.ny * a.g.nx;
+    const float *sig = a.signal + det * a.sig_stride;
+    unsigned *mw = mm.words + ((long long)blockIdx.x * gridDim.y + blockIdx.y) * mm.wpp +
+                   (threadIdx.x >> 5);
+    const int rounds = (t1 - t0 + kBlock - 1) / kBlock;
+    for (int r = 0; r < rounds; r++) {
+        const int t = t0 + r * kBlock + threadIdx.x;
+        const bool live = t < t1;
+        const float s = (!WEIGHT && live) ? __ldg(sig + t) : 0.f;
+        float qb[4] = {1.f, 0.f, 0.f, 0.f};
+        if (live) {
+            const float4 b = __ldg(a.bore32 + t);
+            qb[0] = b.x;
+            qb[1] = b.y;
+            qb[2] = b.z;
+            qb[3] = b.w;
+        }
+        int pix[2] = {0, 0};
+        float pf[3] = {0.f, 0.f, 0.f};
+        bool on = false;
+        const bool ok = live && mixed_pointing<C, P, true, false>(a.g, a.ft, a.mc, qb, qd, nc, T,
+                                                                  Pr, pix, on, pf);
+        const unsigned fails = __ballot_sync(kFull, live && !ok);
+        if (fails && (threadIdx.x & 31) == 0) mw[r * (kBlock / 32)] = fails;
+        int key = -1;
+        if (ok && on) key = P == PX_HP_NT ? pix[0] : pix[0] * a.g.nx + pix[1];
+        float v[NV];
+        tap_values<WEIGHT, NV, true>(s, pf, 1.f, det_wt, v);
+        if (a.accum == SO3G_ACCUM_WARP_RUNS) {
+            flush_runs32<NV>(key, plane, v, mult, vmask, a.map);
+        } else if (key >= 0) {
+            double *p = a.map + key;
+#pragma unroll
+            for (int k = 0; k < NV; k++)
+                if ((vmask >> k) & 1u) atomicAdd(p + mult[k] * plane, f2d(v[k]));
+        }
+    }
+}
+
+// The fallback pass of k_scatter_mx: double-float pointing (float32 spin
+// factors and terms), then the exact float64 pointing.
+template <int C, int P, bool WEIGHT>
+__global__ void __launch_bounds__(kBlock) k_scatter_mx_fix(ScatterArgs a, MxMask mm) {
+    constexpr int NV = WEIGHT ? 6 : 3;
+    int mult[NV];
+    const unsigned vmask = value_slots<WEIGHT>(a.g.ncomp, mult);
+    mx_for_each(a.segs, a.piece, mm, [&](int det, int t) {
+        const float det_wt = a.det_weights ? __ldg(a.det_weights + det) : 1.f;
+        const QuatD ofs = load_quat(a.dets + 4LL * det);
+        const dfl qd[4] = {df_of(ofs.a), df_of(ofs.b), df_of(ofs.c), df_of(ofs.d)};
+        const float T = __ldg(a.resp + 2 * det), Pr = __ldg(a.resp + 2 * det + 1);
+        if (!df_sample<C, P, WEIGHT, false>(a, det, t, qd, T, Pr, det_wt, mult, vmask))
+            exact_sample<C, P, WEIGHT>(a, det, t, ofs, T, Pr, det_wt, mult, vmask);
+    });
+}
+
+// Runs the two passes on a.segs / grid; returns 1 (nothing launched, the
+// caller runs k_scatter) when the pixelization is not eligible, the map
+// index does not fit 31 bits, or the mask cannot be allocated.
+template <int C, int P, bool WEIGHT>
+int scatter_mixed(const ScatterArgs &a, dim3 grid, cudaStream_t stream) {
+    if constexpr (!MxEligible<C, P>::value) {
+        return 1;
+    } else {
+        const long long npix = P == PX_HP_NT ? a.g.npix : (long long)a.g.ny * a.g.nx;
+        if (!a.bore32 || npix >= (1LL << 31)) return 1;
+        MxMask mm;
+        if (!mx_mask_alloc(mm, grid, a.piece, stream)) return 1;
+        k_scatter_mx<C, P, WEIGHT><<<grid, kBlock, 0, stream>>>(a, mm);
+        int rc = after_launch(WEIGHT ? "to_weight_map (mixed)" : "to_map (mixed)");
+        if (rc == SO3G_OK) {
+            k_scatter_mx_fix<C, P, WEIGHT><<<mx_fix_blocks(mm), kBlock, 0, stream>>>(a, mm);
+            rc = after_launch(WEIGHT ? "to_weight_map (mixed fallback)"
+                                     : "to_map (mixed fallback)");
+        }
+        cudaFreeAsync(mm.words, stream);
+        return rc;
+    }
+}
+
+}  // namespace
+
+}  // namespace so3g

@@ -4,7 +4,7 @@
 // own kernel instantiations.
 #pragma once
 
-#include "scatter_kernel.cuh"
+#include "mixed_launch.cuh"
 
 namespace so3g {
 
@@ -20,6 +20,12 @@ struct ScatterLaunch {
         ScatterLaunch *L;
         template <int MODE>
         int go() {
+            if constexpr (MODE == SO3G_POINTING_MIXED) {
+                // Untiled nearest-neighbour maps: the float32 tier alone, its
+                // fallback in a second pass (mixed_launch.cuh).
+                const int rc = scatter_mixed<C, P, WEIGHT>(L->a, L->grid, L->stream);
+                if (rc != 1) return rc;
+            }
             k_scatter<C, P, WEIGHT, MODE><<<L->grid, kBlock, 0, L->stream>>>(L->a);
             return after_launch(WEIGHT ? "to_weight_map" : "to_map");
         }

@@ -19,11 +19,17 @@ Maps are compared pixel by pixel, relative to each pixel's hit-weighted
 scale s_p = sum over the samples hitting p of |signal| * max(|T|, |P|)
 (the sum of the magnitudes of the terms added into p): exact and
 certified pointing to 1e-12 s_p (the float64 summation order), mixed
-pointing to MIXED_PF_BOUND s_p, the bound on a float32 spin factor's
-error, and to 1e-6 of the map's largest |value|.  Signals from from_map are
-compared sample by sample against the per-sample scale sum_c |m_c[p]| *
-max(|T|, |P|): bit for bit for exact and certified nearest-neighbour
-pointing, within the same bounds otherwise.
+pointing to 1e-6 s_p, and to 1e-6 of the map's largest |value|.  Signals
+from from_map are compared sample by sample against the per-sample scale
+sum_c |m_c[p]| * max(|T|, |P|): bit for bit for exact and certified
+nearest-neighbour pointing, within 1e-6 otherwise.
+
+The mixed bound: a float32 spin factor's error is at most MIXED_PF_BOUND
+of P anywhere the float32 tier runs (the worst case sits at its |sin lat|
+< 0.9 guard); on these workloads, which scan near the native equator,
+every spin factor is within 1e-6 of P (measured: <= 3.3e-7 per sample),
+so maps and signals are held to the benchmark spec's 1e-6 per pixel and per
+sample.
 """
 import numpy as np
 import pytest
@@ -43,6 +49,7 @@ MODES = {"exact": _abi.POINTING_EXACT, "certified": _abi.POINTING_CERTIFIED,
 # nearest floats from the double-float path.
 MIXED_PF_BOUND = 2e-5
 RTOL_EXACT = 1e-12
+RTOL_MIXED = 1e-6
 RTOL_GLOBAL_MIXED = 1e-6
 
 
@@ -207,7 +214,7 @@ def test_cfg1_pixels_every_mode(orc, gpulib, cfg1):
 def test_cfg1_to_map_per_pixel(orc, gpulib, cfg1, name):
     p, q, d, resp, sig = cfg1
     mode = MODES[name]
-    rtol = MIXED_PF_BOUND if name == "mixed" else RTOL_EXACT
+    rtol = RTOL_MIXED if name == "mixed" else RTOL_EXACT
     eng, want, rel, glob = _to_map_case(orc, p, q, d, resp, sig, mode, rtol)
     print("cfg1 %s to_map: max error / hit scale %.2e, / max|map| %.2e" % (name, rel, glob))
     if name == "mixed":
@@ -216,7 +223,7 @@ def test_cfg1_to_map_per_pixel(orc, gpulib, cfg1, name):
     m = want.reshape((3,) + tuple(eng._pix_shape()))
     r = _from_map_case(orc, eng, q, d, resp, m, mode, exact_bits=name != "mixed")
     print("cfg1 %s from_map: max error / sample scale %.2e" % (name, r))
-    assert r <= MIXED_PF_BOUND
+    assert r <= RTOL_MIXED
 
 
 @pytest.mark.parametrize("name", list(MODES))
@@ -235,7 +242,7 @@ def test_cfg1_to_weight_map_per_pixel(orc, gpulib, cfg1, name):
     orc.to_weight_map(_pz(eng, _abi.POINTING_EXACT), q, d, resp, None, want)
     scale = _hit_scale(orc, eng, q, d, resp, sig, 3, weight=True)
     # Products of two spin factors: twice the single-factor bound.
-    rtol = 2 * MIXED_PF_BOUND if name == "mixed" else RTOL_EXACT
+    rtol = 2 * RTOL_MIXED if name == "mixed" else RTOL_EXACT
     rel, glob = _check_map(got.cpu().numpy(), want, scale, 9, rtol, "to_weight_map")
     print("cfg1 %s to_weight_map: max error / hit scale %.2e, / max|map| %.2e" %
           (name, rel, glob))
@@ -255,7 +262,7 @@ def test_cfg2_slice(orc, gpulib, name):
     print("cfg2 slice %s: pixel mismatches %d of %d" % (name, n_bad, want.size))
     assert n_bad == 0
     del got, want
-    rtol = MIXED_PF_BOUND if name == "mixed" else RTOL_EXACT
+    rtol = RTOL_MIXED if name == "mixed" else RTOL_EXACT
     eng, want, rel, glob = _to_map_case(orc, p, q, d, resp, sig, mode, rtol)
     print("cfg2 slice %s to_map: max error / hit scale %.2e, / max|map| %.2e" %
           (name, rel, glob))
@@ -264,7 +271,7 @@ def test_cfg2_slice(orc, gpulib, name):
     m = want.reshape((3,) + tuple(eng._pix_shape()))
     r = _from_map_case(orc, eng, q, d, resp, m, mode, exact_bits=name != "mixed")
     print("cfg2 slice %s from_map: max error / sample scale %.2e" % (name, r))
-    assert r <= MIXED_PF_BOUND
+    assert r <= RTOL_MIXED
 
 
 # -- cfg3: HEALPix nside 1024, 4e7 samples -----------------------------------------
@@ -311,7 +318,7 @@ def test_cfg3_slice_maps(orc, gpulib):
     c, p, q, d, resp = _workload("cfg3", n_det=4, every=500, n_time=1_000_000)
     sig = _signal(len(d), c["n_time"], seed=3)
     for name in ("certified", "mixed"):
-        rtol = MIXED_PF_BOUND if name == "mixed" else RTOL_EXACT
+        rtol = RTOL_MIXED if name == "mixed" else RTOL_EXACT
         eng, want, rel, glob = _to_map_case(orc, p, q, d, resp, sig, MODES[name], rtol)
         print("cfg3 slice %s to_map: max error / hit scale %.2e, / max|map| %.2e" %
               (name, rel, glob))

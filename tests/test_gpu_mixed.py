@@ -14,7 +14,14 @@ ARCMIN = np.pi / 180 / 60
 MODES = (_abi.POINTING_EXACT, _abi.POINTING_MIXED)
 
 
-def _probe(eng, q, dets, resp, tiled, ncomp=3):
+# Spin-factor error bounds of the float32 tier, relative to P.  Anywhere
+# the tier runs (|sin lat| < 0.9): PF_BOUND_GUARD, reached only near that
+# guard; on scans near the native equator (the benchmark geometry): 1e-6.
+PF_BOUND_GUARD = 2e-5
+PF_BOUND_SCAN = 1e-6
+
+
+def _probe(eng, q, dets, resp, tiled, ncomp=3, pf_bound=PF_BOUND_SCAN):
     import torch
     qd, dd, rd = (torch.from_numpy(x).cuda() for x in (q, dets, resp))
     maps = _probe_maps(eng, tiled, ncomp)
@@ -27,7 +34,7 @@ def _probe(eng, q, dets, resp, tiled, ncomp=3):
     assert bits_equal(ex[0], mx[0])
     # Spin factors: float32 evaluations.
     for a, b in zip(ex[1:], mx[1:]):
-        assert np.abs(a - b).max() <= 2e-5
+        assert np.abs(a - b).max() <= pf_bound
         assert np.abs(a - b).mean() <= 2e-7
     return ex
 
@@ -72,7 +79,7 @@ def test_mixed_wide_map_seam_and_caps():
     resp = np.ones((1, 2), np.float32)
     p, eng = _engine((200, 200), 60 * ARCMIN, False)
     eng2 = type(eng)((200, 400, 0.9 * np.pi / 180, -0.9 * np.pi / 180, 100.5, 200.5))
-    _probe(eng2, q, dets, resp, False)
+    _probe(eng2, q, dets, resp, False, pf_bound=PF_BOUND_GUARD)
 
 
 @pytest.mark.parametrize("tiled", [False, True])
@@ -122,7 +129,7 @@ def _probe_hp(eng, q, dets, resp, tiled):
     ex, mx = out[_abi.POINTING_EXACT], out[_abi.POINTING_MIXED]
     assert bits_equal(ex[0], mx[0])
     for a, b in zip(ex[1:], mx[1:]):
-        assert np.abs(a - b).max() <= 2e-5
+        assert np.abs(a - b).max() <= pf_bound
         assert np.abs(a - b).mean() <= 2e-7
 
 
@@ -215,5 +222,5 @@ def test_mixed_zenithal_whole_sky(proj):
     q = _quats_at(lon, lat, rng.uniform(0, np.pi, n))
     dets = np.array([[1., 0., 0., 0.], [np.cos(0.3), 0., 0., np.sin(0.3)]])
     resp = np.array([[1., 1.], [0.7, 0.45]], np.float32)
-    res = _probe(eng, q, dets, resp, False)
+    res = _probe(eng, q, dets, resp, False, pf_bound=PF_BOUND_GUARD)
     assert (res[0] > 0).mean() > 0.05

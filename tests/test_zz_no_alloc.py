@@ -171,14 +171,15 @@ def test_noalloc_rejects_oversize():
     assert "at most 65536 sample segments" in _abi.last_error()
 
 
-def _noalloc_case(lib, c, mode, seg=None):
-    """so3g_proj_to_map_noalloc of a helpers.Case in pointing mode `mode`;
-    returns the flat map and its tile offsets (None if untiled)."""
+def _noalloc_case(lib, c, mode, populate=None, seg=None):
+    """so3g_proj_to_map_noalloc of a helpers.Case in pointing mode `mode`
+    (tiled: the tiles in `populate`, or all); returns the flat map and its
+    tile offsets (None if untiled)."""
     import torch
     from so3g_gb300 import _abi
     from helpers import oracle_map
     dev = torch.device("cuda", torch.cuda.current_device())
-    flat, offs = oracle_map(c.blank((c.ncomp,)))
+    flat, offs = oracle_map(c.blank((c.ncomp,), populate))
     m = torch.zeros(flat.size, dtype=torch.float64, device=dev)
     q, d, r, s = (torch.from_numpy(np.ascontiguousarray(x)).to(dev)
                   for x in (c.bore, c.dets, c.resp, c.signal))
@@ -206,22 +207,25 @@ def test_noalloc_every_pointing_mode_against_oracle(orc, kind):
     from helpers import Case, oracle_map
     lib = _abi.lib()
     assert lib.so3g_init() == 0
+    active = None
     if kind == "HP_NEST_TILED":
         c = Case(orc, coord="CAR", hp=(256, True, 8), tiled=True, n_det=6, n_time=6000,
                  seed=21)
         hits = np.array(c.eng.tile_hits(c.bore, c.dets))
+        active = [int(i) for i in np.nonzero(hits)[0]]
+        # The engine's own maps (to_map(None, ...)) hold the active tiles.
         c = Case(orc, coord="CAR", hp=(256, True, 8), tiled=True, n_det=6, n_time=6000,
-                 seed=21, active=[int(i) for i in np.nonzero(hits)[0]])
+                 seed=21, active=active)
     else:
         c = Case(orc, coord=kind, n_det=6, n_time=6000, seed=22)
-    want, woffs = oracle_map(c.blank((c.ncomp,)))
+    want, woffs = oracle_map(c.blank((c.ncomp,), active))
     orc.to_map(c.pz, c.bore, c.dets, c.resp, c.signal, None, want, woffs)
     scale = np.abs(want).max()
     assert scale > 0
     for mode, tol in ((_abi.POINTING_EXACT, 1e-12), (_abi.POINTING_CERTIFIED, 1e-12),
                       (_abi.POINTING_MIXED, 1e-6)):
         for _ in range(2):
-            got, offs = _noalloc_case(lib, c, mode)
+            got, offs = _noalloc_case(lib, c, mode, active)
             assert offs is None or np.array_equal(offs, woffs)
             assert np.abs(got - want).max() <= tol * scale, (mode, np.abs(got - want).max())
         c.eng.pointing = mode
