@@ -9,10 +9,13 @@ does.
 
 Parity pin: the oracle's trig tables and HEALPix ang2pix are checked
 against golden vectors generated from the reference's own so_linterp.h and
-healpix_bare.c (tests/golden/), and its pointing/projection against the
-reference's analytic known-answer tests (tests/test_oracle_kat.py).  The
-rest of Projection.cxx could not be compiled standalone (boost.python,
-spt3g), so its restatement is pinned by those known answers only.
+healpix_bare.c (tests/golden/), its pointing/projection against the
+reference's analytic known-answer tests (tests/test_oracle_kat.py), and
+every engine method against the reference's own ProjectionEngine compiled
+from src/Projection.cxx with stand-in boost.python/spt3g headers
+(oracle/ref_engine.cpp, tests/test_oracle_reference.py): bit for bit.
+The last bit of boost's quaternion product is not pinned (boost is not
+installed; both sum each component left to right).
 """
 import ctypes
 

@@ -24,6 +24,7 @@ REFERENCE = os.environ.get(
 
 ORACLE_SO = os.path.join(HERE, "_build", "libproj_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libref_parts.so")
+REF_ENGINE_SO = os.path.join(HERE, "_ref", "libref_engine.so")
 
 
 def _stale(target, sources):
@@ -71,6 +72,36 @@ def build_ref(force=False):
     return REF_SO
 
 
+def ref_sources_present():
+    return os.path.exists(os.path.join(REFERENCE, "src", "Projection.cxx"))
+
+
+def build_ref_engine(force=False):
+    """Compiles the reference's src/Projection.cxx, read in place from the
+    reference checkout, with the stand-in headers of oracle/refstub and the
+    wrapper oracle/ref_engine.cpp into oracle/_ref/libref_engine.so (a
+    library loaded into Python with ctypes.PyDLL).  Returns None where the
+    reference checkout is absent."""
+    if not ref_sources_present():
+        return None
+    import sysconfig
+    import numpy
+    stub = os.path.join(HERE, "refstub")
+    srcs = [os.path.join(HERE, "ref_engine.cpp"), os.path.join(HERE, "ref_numpy.cpp")]
+    deps = srcs + [os.path.join(REFERENCE, "src", "Projection.cxx")] + [
+        os.path.join(d, f) for d, _, fs in os.walk(stub) for f in fs]
+    if force or _stale(REF_ENGINE_SO, deps):
+        os.makedirs(os.path.dirname(REF_ENGINE_SO), exist_ok=True)
+        tmp = REF_ENGINE_SO + ".tmp"
+        _run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
+              "-DNDEBUG", "-I", stub, "-I", os.path.join(REFERENCE, "include"),
+              "-I", os.path.join(REFERENCE, "src"), "-I", sysconfig.get_paths()["include"],
+              "-I", numpy.get_include()] + srcs + ["-o", tmp])
+        os.replace(tmp, REF_ENGINE_SO)
+    return REF_ENGINE_SO
+
+
 if __name__ == "__main__":
     print(build_oracle())
     print(build_ref())
+    print(build_ref_engine())

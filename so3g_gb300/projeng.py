@@ -116,8 +116,10 @@ def _match_shape(name, pattern, shape):
             break
         i += 1
     if i != len(pattern) or j != len(shape):
-        raise shape_error(name, "Expected %s but got %s" % (_shape_string(pattern),
-                                                           _shape_string(shape)))
+        # numpy_assist.h:201-206 ends the detail with its own period, to
+        # which the shape_exception message adds another.
+        raise shape_error(name, "Expected %s but got %s." % (_shape_string(pattern),
+                                                            _shape_string(shape)))
 
 
 def as_array(obj, name, tname, shape=None, optional=False):
@@ -596,8 +598,16 @@ class _MapArg:
         self.host = None
         self._host_tiles = None
         self.dev = None
+        # The reference checks the component axes of a flat map but not its
+        # pixel axes (src/Projection.cxx:867-879, 1055-1082: (ncomp, *, *));
+        # a map of another pixel shape is then written out of bounds there.
+        # The reference's check runs first, with its message, then the
+        # pixel axes are checked too.
+        ref_pix = (-1, -1) if not eng._hp else None
         if not eng._tiled:
             arr = as_array(obj, name, "float64")
+            if ref_pix:
+                _match_shape(name, tuple(lead) + ref_pix, tuple(arr.shape))
             _match_shape(name, tuple(lead) + eng._pix_shape(), tuple(arr.shape))
             self._arr = arr
             return
@@ -613,6 +623,8 @@ class _MapArg:
                     raise tiling_error(i, "Projector expects tile but it is missing.")
                 continue
             arr = as_array(t, name, "float64")
+            if ref_pix:
+                _match_shape(name, tuple(lead) + ref_pix, tuple(arr.shape))
             _match_shape(name, tuple(lead) + eng._tile_pix_shape(i), tuple(arr.shape))
             present.append((i, arr))
         self._present = present

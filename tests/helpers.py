@@ -76,6 +76,7 @@ class Case:
             name = "ProjEng_HP_%s_%s" % (SPINS[ncomp], "Tiled" if tiled else "NonTiled")
             args = (nside, int(nest), nside_tile, active)
             self.eng = getattr(so3g_gb300, name)(args)
+            self.name, self.args = name, args
         else:
             probe = so3g_gb300.ProjEng_CAR_TQU_NonTiled((1, 1, 1., 1., 1., 1.))
             pz = probe._pz()
@@ -86,7 +87,9 @@ class Case:
                 args = args + tuple(tile_shape)
                 if active is not None:
                     args = args + (active,)
-            self.eng = getattr(so3g_gb300, engine_name(coord, ncomp, tiled, bilinear))(args)
+            self.name = engine_name(coord, ncomp, tiled, bilinear)
+            self.args = args
+            self.eng = getattr(so3g_gb300, self.name)(args)
         self.pz = self.eng._pz()
 
     def all_tiles(self):
