@@ -80,9 +80,14 @@ def test_validation_errors_precede_device_work():
     d[2, 1] = np.nan
     with pytest.raises(ValueError, match=r"Pointing offset error: nan found at index 2."):
         e.to_map(None, bore, d, resp, sig)
+    # The reference's own check (component axis; its message), then the
+    # pixel axes, which the reference leaves unchecked.
     with pytest.raises(RuntimeError, match=r"Buffer 'map' has incompatible shape: "
-                                           r"Expected \(3, 10, 20\) but got \(1, 10, 20\)."):
+                                           r"Expected \(3, \*, \*\) but got \(1, 10, 20\)\.\."):
         e.to_map(np.zeros((1, 10, 20)), bore, dets, resp, sig)
+    with pytest.raises(RuntimeError, match=r"Buffer 'map' has incompatible shape: "
+                                           r"Expected \(3, 10, 20\) but got \(3, 10, 21\)\.\."):
+        e.to_map(np.zeros((3, 10, 21)), bore, dets, resp, sig)
     with pytest.raises(RuntimeError, match="must contain \\(n_det\\) vectors"):
         e.to_map(None, bore, dets, resp, sig[:2])
     with pytest.raises(RuntimeError, match=r"Buffer 'signal' has incompatible shape"):
