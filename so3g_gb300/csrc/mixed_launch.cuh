@@ -31,8 +31,8 @@ namespace {
 // flush_runs (device.cuh) with a 32-bit pixel key (-1: nothing to add):
 // runs of equal keys across the warp are summed in compensated float32 and
 // flushed with one float64 atomic per run and value; a warp with at least
-// DIRECT_RUNS runs adds every term with its own atomic.
-template <int NV>
+// DIRECT runs adds every term with its own atomic.
+template <int NV, int DIRECT>
 __device__ __forceinline__ void flush_runs32(int key, long long plane, float (&v)[NV],
                                              const int (&mult)[NV], unsigned vmask,
                                              double *map) {
@@ -40,7 +40,7 @@ __device__ __forceinline__ void flush_runs32(int key, long long plane, float (&v
     const int prev = __shfl_up_sync(kFull, key, 1);
     const bool head = (lane == 0) || (key != prev);
     const unsigned heads = __ballot_sync(kFull, head);
-    if (__popc(heads) >= kDirectRuns) {
+    if (__popc(heads) >= DIRECT) {
         if (key >= 0) {
             double *p = map + key;
 #pragma unroll
@@ -78,6 +78,11 @@ __device__ __forceinline__ void flush_runs32(int key, long long plane, float (&v
             if ((vmask >> k) & 1u) atomicAdd(p + mult[k] * plane, f2d(v[k]) + f2d(e[k]));
     }
 }
+
+// to_weight_map: a warp adds its terms one by one only when it has at
+// least this many runs of equal pixels (six values per sample make the
+// per-run reduction pay sooner than to_map's three).
+constexpr int kMxDirectRunsWeight = 12;
 
 // The main pass.  Block (x, y): piece y of segment x, in rounds of kBlock
 // samples (lane = sample).  Needs the float32 boresight copy (a.bore32).
@@ -127,7 +132,8 @@ __global__ void __launch_bounds__(kBlock, kMxBlocksPerSM) k_scatter_mx(ScatterAr
         float v[NV];
         tap_values<WEIGHT, NV, true>(s, pf, 1.f, det_wt, v);
         if (a.accum == SO3G_ACCUM_WARP_RUNS) {
-            flush_runs32<NV>(key, plane, v, mult, vmask, a.map);
+            flush_runs32<NV, WEIGHT ? kMxDirectRunsWeight : kDirectRuns>(key, plane, v, mult,
+                                                                         vmask, a.map);
         } else if (key >= 0) {
             double *p = a.map + key;
 #pragma unroll

@@ -117,7 +117,7 @@ def test_mixed_maps_within_tolerance(tiled):
         assert np.abs(a - b).max() <= 1e-6 * np.abs(a).max()
 
 
-def _probe_hp(eng, q, dets, resp, tiled):
+def _probe_hp(eng, q, dets, resp, tiled, pf_bound=PF_BOUND_GUARD):
     import torch
     from test_gpu_certified import _hp_probe_maps
     qd, dd, rd = (torch.from_numpy(x).cuda() for x in (q, dets, resp))
