@@ -75,6 +75,8 @@ def parse():
     ap.add_argument("--no-fp64-path", action="store_true")
     ap.add_argument("--no-precomp", action="store_true",
                     help="leave out the precomputed-pointing leg of the default line")
+    ap.add_argument("--no-legs", action="store_true",
+                    help="leave out the HEALPix, differentiable and batched legs")
     ap.add_argument("--ops", default="to_map,from_map",
                     help="operations timed in a step (profiling runs pick one)")
     ap.add_argument("--batch-scale", type=float, default=1.0,
@@ -322,7 +324,10 @@ def algorithmic_bytes(c, op):
 # ---------------------------------------------------------------------------
 # Our implementation.
 
-def run_ours(args, c, rank, world):
+def run_ours(args, c, rank, world, lean=False):
+    """Times args.steps steps of the workload on this rank's GPU; lean:
+    the timed steps only (no certified / float64 / accuracy / weight-map /
+    end-to-end side measurements)."""
     import torch
     import so3g_gb300
     from so3g_gb300 import _abi
@@ -409,6 +414,9 @@ def run_ours(args, c, rank, world):
                                         pointing=mode)
     ms = max_over_ranks(ms, dev)
     res = {"ms_per_step": ms, "op_ms": op_ms, "launches": launches, "clocks": clocks}
+    if lean:
+        del sig, out
+        return res, N
     if world == 1 and c["kind"] != "zea_grad" and mode != _abi.POINTING_CERTIFIED:
         # The bit-exact certified mode, for comparison.
         msc, opc, _, _ = timed(_abi.ACCUM_WARP_RUNS, max(1, args.steps // 2), 1,
@@ -756,7 +764,56 @@ def run_batch(args, c):
                          "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
                          "peak_kind": kind, "to_map_ms": ms_tm},
             "clocks": clocks, "gpu_launches": graph.launches * args.steps}
-    print(json.dumps(line))
+    return line
+
+
+# ---------------------------------------------------------------------------
+# The other workloads, as legs of the default line.
+
+def _free_gpu():
+    import gc
+    import torch
+    gc.collect()
+    torch.cuda.empty_cache()
+
+
+def workload_leg(args, name, steps=3, warmup=3):
+    """The mixed-pointing step of workload `name` (cfg3: HEALPix to_map +
+    from_map; cfg5: differentiable from_map forward + backward) at full
+    size, with its HBM roofline."""
+    a = argparse.Namespace(**vars(args))
+    a.config, a.steps, a.warmup, a.tiled, a.pointing = name, steps, warmup, False, "mixed"
+    a.ops = "to_map,from_map"
+    c = config(a)
+    _free_gpu()
+    res, N = run_ours(a, c, 0, 1, lean=True)
+    _free_gpu()
+    metric, workload, map_shape = describe(c)
+    hbm, kind = peaks()
+    op = "from_map_fwd_bwd" if c["kind"] == "zea_grad" else "to_map"
+    B = algorithmic_bytes(c, op)
+    ach = B * N / (res["op_ms"][op] * 1e-3) / 1e9
+    return {"metric": metric, "workload": workload, "value": N / (res["ms_per_step"] * 1e-3),
+            "unit": "samples/s", "steps": steps, "warmup": warmup,
+            "ms_per_step": res["ms_per_step"], "op_ms": res["op_ms"],
+            "roofline": {"bound": "hbm", "kernel": op, "achieved": ach, "peak": hbm,
+                         "unit": "GB/s", "frac": ach / hbm, "traffic": None,
+                         "bytes_per_sample": B, "peak_kind": kind},
+            "clocks": res["clocks"], "gpu_launches": int(res["launches"])}
+
+
+def batch_leg(args, steps=3, warmup=3):
+    """cfg4: 16 observations into one map, the tuned graph against 16
+    sequential plain calls."""
+    a = argparse.Namespace(**vars(args))
+    a.steps, a.warmup, a.pointing, a.batch_scale = steps, warmup, "mixed", 1.0
+    _free_gpu()
+    line = run_batch(a, dict(CONFIGS["cfg4"]))
+    _free_gpu()
+    for k in ("tune_log", "n_gpus", "vs_baseline", "data", "dtype", "scaling",
+              "higher_is_better"):
+        line.pop(k, None)
+    return line
 
 
 # ---------------------------------------------------------------------------
@@ -932,7 +989,8 @@ def cpu_baseline(c):
 def main():
     args = parse()
     if args.config == "cfg4" and args.impl == "ours":
-        return run_batch(args, dict(CONFIGS["cfg4"]))
+        print(json.dumps(run_batch(args, dict(CONFIGS["cfg4"]))))
+        return
     c = config(args)
     if args.precomp and args.impl == "ours":
         return run_precomp(args, c)
@@ -1021,6 +1079,10 @@ def main():
                            "step": "Precomp to_map + from_map on pointing_matrix output "
                                    "(pixel indices bit-exact, spin factors as the "
                                    "certified path)"}
+    if world == 1 and args.config == "cfg2" and not args.no_legs:
+        # The other benchmark workloads at full size, mixed pointing.
+        line["legs"] = {"hp": workload_leg(args, "cfg3"), "grad": workload_leg(args, "cfg5"),
+                        "batch": batch_leg(args)}
     if world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(c)
     print(json.dumps(line))

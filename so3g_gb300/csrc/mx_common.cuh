@@ -29,8 +29,9 @@ struct MxEligible {
 struct MxMask {
     unsigned *words;
     long long n_words;
-    int wpp;      // words per piece: (piece / kBlock) rounds x (kBlock / 32) warps
-    int gy;       // pieces per segment (grid.y of the main kernel)
+    int wpp;         // words per piece: (piece / kBlock) rounds x (kBlock / 32) warps
+    int wpp_shift;   // log2(wpp): pieces are powers of two
+    int gy;          // pieces per segment (grid.y of the main kernel)
 };
 
 // Position of the k-th (0-based) set bit of w (w has more than k set bits).
@@ -39,12 +40,13 @@ __device__ __forceinline__ int nth_bit(unsigned w, int k) {
     return __ffs(w) - 1;
 }
 
-// (det, t) of bit `bit` of mask word `word`.
+// (det, t) of bit `bit` of mask word `word`.  Integer shifts and one
+// 32-bit division: 64-bit division would run on the float64 pipe.
 __device__ __forceinline__ void mx_sample(const Segs &segs, int piece, const MxMask &mm,
                                           long long word, int bit, int &det, int &t) {
-    const long long blk = word / mm.wpp;
-    const int rem = (int)(word - blk * mm.wpp);
-    const int x = (int)(blk / mm.gy), y = (int)(blk - (long long)x * mm.gy);
+    const unsigned blk = (unsigned)(word >> mm.wpp_shift);   // < 2^31 blocks
+    const int rem = (int)(word & (long long)(mm.wpp - 1));
+    const unsigned x = blk / (unsigned)mm.gy, y = blk - x * (unsigned)mm.gy;
     int s0 = 0;
     if (segs.seg) {
         det = __ldg(segs.seg + 3 * x);
@@ -100,7 +102,11 @@ __device__ __forceinline__ void mx_for_each(const Segs &segs, int piece, const M
 // allocation fails.
 inline bool mx_mask_alloc(MxMask &mm, dim3 grid, int piece, cudaStream_t stream) {
     mm.wpp = (piece / kBlock) * (kBlock / 32);
+    mm.wpp_shift = 0;
+    while ((1 << mm.wpp_shift) < mm.wpp) mm.wpp_shift++;
+    if ((1 << mm.wpp_shift) != mm.wpp) return false;   // pieces are powers of two
     mm.gy = (int)grid.y;
+    if ((long long)grid.x * grid.y >= (1LL << 31)) return false;   // mx_sample's 32-bit blocks
     mm.n_words = (long long)grid.x * grid.y * mm.wpp;
     mm.words = nullptr;
     if (cudaMallocAsync(reinterpret_cast<void **>(&mm.words),
