@@ -79,11 +79,6 @@ __device__ __forceinline__ void flush_runs32(int key, long long plane, float (&v
     }
 }
 
-// to_weight_map: a warp adds its terms one by one only when it has at
-// least this many runs of equal pixels (six values per sample make the
-// per-run reduction pay sooner than to_map's three).
-constexpr int kMxDirectRunsWeight = 12;
-
 // The main pass.  Block (x, y): piece y of segment x, in rounds of kBlock
 // samples (lane = sample).  Needs the float32 boresight copy (a.bore32).
 template <int C, int P, bool WEIGHT>
@@ -132,8 +127,7 @@ __global__ void __launch_bounds__(kBlock, kMxBlocksPerSM) k_scatter_mx(ScatterAr
         float v[NV];
         tap_values<WEIGHT, NV, true>(s, pf, 1.f, det_wt, v);
         if (a.accum == SO3G_ACCUM_WARP_RUNS) {
-            flush_runs32<NV, WEIGHT ? kMxDirectRunsWeight : kDirectRuns>(key, plane, v, mult,
-                                                                         vmask, a.map);
+            flush_runs32<NV, kDirectRuns>(key, plane, v, mult, vmask, a.map);
         } else if (key >= 0) {
             double *p = a.map + key;
 #pragma unroll
