@@ -26,7 +26,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-f
 UNITS = ["api.cu", "pointing.cu", "scatter.cu", "scatter_weight.cu", "gather.cu", "precomp.cu",
          "noalloc.cu", "batch.cu", "batch_weight.cu", "sightline.cu", "ranges.cu"]
 HEADERS = ["device.cuh", "host.h", "scatter_kernel.cuh", "scatter_launch.cuh", "batch_launch.cuh",
-           "fastpoint.cuh", "mixedpoint.cuh", "mixed_launch.cuh", "mx_common.cuh"]
+           "fastpoint.cuh", "mixedpoint.cuh", "mixed_launch.cuh", "mx_common.cuh", "interp_point.cuh"]
 
 
 def nvcc():

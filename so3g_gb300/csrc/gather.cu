@@ -13,6 +13,7 @@
 // exact path's.
 
 #include "host.h"
+#include "interp_point.cuh"
 #include "mx_common.cuh"
 
 namespace so3g {
@@ -528,6 +529,119 @@ __global__ void __launch_bounds__(kBlock) k_from_map_mx_fix(GatherArgs a, MxMask
     });
 }
 
+// The chunked from_map for CAR maps (interp_point.cuh), laid out as
+// k_scatter_ix: the map read from its float32 copy, the signal updated
+// where the sample is certified and on the map, the others marked.
+__global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
+    k_from_map_ix(GatherArgs a, MxMask mm, const IxBore *ixb) {
+    __shared__ IxParams sp[kBlock / 32][32];
+    int det, t0, t1;
+    if (!seg_piece(a.segs, a.piece, det, t0, t1)) return;
+    const QuatD ofs = load_quat(a.dets + 4LL * det);
+    const dfl qd[4] = {df_of(ofs.a), df_of(ofs.b), df_of(ofs.c), df_of(ofs.d)};
+    const float q32[4] = {d2f_round(ofs.a), d2f_round(ofs.b), d2f_round(ofs.c),
+                          d2f_round(ofs.d)};
+    const float T = __ldg(a.resp + 2 * det), Pr = __ldg(a.resp + 2 * det + 1);
+    const int nc = a.g.ncomp;
+    float *sig = a.signal + det * a.sig_stride;
+    unsigned *mwb = mm.words + ((long long)blockIdx.x * gridDim.y + blockIdx.y) * mm.wpp;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int j0 = t0 / kIxLen, j1 = (t1 - 1) / kIxLen + 1;
+    for (int g = j0 + warp * 32; g < j1; g += (kBlock / 32) * 32) {
+        if (g + lane < j1) ix_setup(a, ixb, g + lane, a.segs.n_time, qd, q32, sp[warp][lane]);
+        __syncwarp();
+        const int nch = min(32, j1 - g);
+        for (int k = 0; k < nch; k++) {
+#pragma unroll
+            for (int h = 0; h < kIxLen / 32; h++) {
+                const int tw = (g + k) * kIxLen + h * 32;
+                const int t = tw + lane;
+                const bool live = t >= t0 && t < t1;
+                // Loaded before the pointing, so that its latency overlaps it.
+                const float s_in = live ? sig[t] : 0.f;
+                int key = 0;
+                bool on = false;
+                float pf[3];
+                const bool ok = ix_eval(sp[warp][k], t, a.g, a.mc, nc, T, Pr, key, on, pf) &&
+                                live;
+                const unsigned fails = __ballot_sync(kFull, live && !ok);
+                if (fails && lane == 0) mwb[(tw - t0) / 32] = fails;
+                if (ok && on) {
+                    const float4 m = __ldg(a.map32 + key);
+                    // float32 terms (the mixed-precision contract).
+                    float sv = fmaf(m.x, pf[0], s_in);
+                    if (nc > 1) sv = fmaf(m.y, pf[1], sv);
+                    if (nc > 2) sv = fmaf(m.z, pf[2], sv);
+                    sig[t] = sv;
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Fallback pass of k_from_map_ix: the float32 tier, then the double-float
+// pointing (float32 spin factors and terms), then the exact float64 one.
+__global__ void __launch_bounds__(kBlock) k_from_map_ix_fix(GatherArgs a, MxMask mm) {
+    constexpr int C = SO3G_COORD_CAR, P = PX_FLAT_NT_NN;
+    const int nc = a.g.ncomp;
+    mx_for_each(a.segs, a.piece, mm, [&](int det, int t) {
+        const QuatD ofs = load_quat(a.dets + 4LL * det);
+        const float T = __ldg(a.resp + 2 * det), Pr = __ldg(a.resp + 2 * det + 1);
+        const float q32[4] = {d2f_round(ofs.a), d2f_round(ofs.b), d2f_round(ofs.c),
+                              d2f_round(ofs.d)};
+        float qb[4];
+        load_bore_f32(a.bore32, a.bore, t, qb);
+        int pix[2];
+        float pf[3] = {0.f, 0.f, 0.f};
+        bool on = false;
+        if (mixed_pointing<C, P, true, false>(a.g, a.ft, a.mc, qb, q32, nc, T, Pr, pix, on,
+                                              pf)) {
+            if (on) {
+                float *sp = a.signal + det * a.sig_stride + t;
+                const float4 m = __ldg(a.map32 + (pix[0] * a.g.nx + pix[1]));
+                float sv = fmaf(m.x, pf[0], *sp);
+                if (nc > 1) sv = fmaf(m.y, pf[1], sv);
+                if (nc > 2) sv = fmaf(m.z, pf[2], sv);
+                *sp = sv;
+            }
+            return;
+        }
+        const dfl qd[4] = {df_of(ofs.a), df_of(ofs.b), df_of(ofs.c), df_of(ofs.d)};
+        if (!df_gather<C, P>(a, det, t, qd, T, Pr)) exact_gather<C, P>(a, det, t, ofs, T, Pr);
+    });
+}
+
+// The chunked from_map for CAR maps with the untiled nearest-neighbour
+// pixelizor; returns 1 (nothing launched) where it does not apply.
+template <int C, int P>
+int gather_interp(const GatherArgs &a, dim3 grid, cudaStream_t stream) {
+    if constexpr (!(C == SO3G_COORD_CAR && P == PX_FLAT_NT_NN)) {
+        return 1;
+    } else {
+        const long long npix = (long long)a.g.ny * a.g.nx;
+        if (a.segs.seg || a.segs.n_time < 2 || !a.map32 || npix >= (1LL << 31) ||
+            a.piece % kIxLen)
+            return 1;
+        IxBore *ixb = ix_bore_models(a.bore, a.segs.n_time, stream);
+        if (!ixb) return 1;
+        MxMask mm;
+        if (!mx_mask_alloc(mm, grid, a.piece, stream)) {
+            cudaFreeAsync(ixb, stream);
+            return 1;
+        }
+        k_from_map_ix<<<grid, kBlock, 0, stream>>>(a, mm, ixb);
+        int rc = after_launch("from_map (chunked)");
+        if (rc == SO3G_OK) {
+            k_from_map_ix_fix<<<mx_fix_blocks(mm), kBlock, 0, stream>>>(a, mm);
+            rc = after_launch("from_map (chunked fallback)");
+        }
+        cudaFreeAsync(mm.words, stream);
+        cudaFreeAsync(ixb, stream);
+        return rc;
+    }
+}
+
 // Runs the two passes; returns 1 (nothing launched: the caller runs
 // k_from_map) when the pixelization is not eligible, the map has 2^31
 // pixels or more, a float32 copy is missing, or the mask cannot be
@@ -537,6 +651,8 @@ int gather_mixed(const GatherArgs &a, dim3 grid, cudaStream_t stream) {
     if constexpr (!MxEligible<C, P>::value) {
         return 1;
     } else {
+        const int ri = gather_interp<C, P>(a, grid, stream);
+        if (ri != 1) return ri;
         const long long npix = P == PX_HP_NT ? a.g.npix : (long long)a.g.ny * a.g.nx;
         if (!a.bore32 || !a.map32 || npix >= (1LL << 31)) return 1;
         MxMask mm;

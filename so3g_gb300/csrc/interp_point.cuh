@@ -1,0 +1,353 @@
+// interp_point.cuh -- chunked pointing for the mixed mode of CAR maps with
+// the untiled nearest-neighbour pixelizor: the pointing of 64 consecutive
+// samples of a detector from one model, with a certified bound.
+//
+// The boresight of a chunk [ta, tb] (tb = ta + 64, or the last sample) is
+// modelled by the quadratic through its samples at ta, the middle and tb,
+//   Q(s) = q(ta) + s D1 + s^2 D2,   s = (t - ta) / (tb - ta),
+// and E = max over the chunk's samples of |q(t) - Q(s)| is measured from
+// the data (k_ix_bore, float64, once per call for all detectors).  For a
+// detector q_d, q(t) (x) q_d = A0 + s A1 + s^2 A2 + e, |e| <= E |q_d|, with
+// A_k = D_k (x) q_d.  The reference's coordinates are quadratic forms of
+// that quaternion (Pointer<ProjCAR>::GetCoords, src/Projection.cxx:479-507):
+//   w = X + iY = (ca + db) + i(cd - ab),  lon = atan2(Y, X)
+//   Z = a^2 - b^2 - c^2 + d^2,            lat = asin(Z)
+//   v = Nc + iNs = (ac - bd) + i(cd + ab), the spin factors P v^2 / |v|^2
+// so along the model each is a polynomial in s, of degree 4 with its s^3
+// and s^4 coefficients negligible (|A2| ~ 1e-6): per sample,
+//   lon = lon(ta) + arg(1 + z),  z = c1 s + c2 s^2 (c_k = W_k / W_0)
+//         ~ lon(ta) + Im z - Re z Im z                   (|z| < 0.05)
+//   lat = lat(ta) + k1 dZ + k2 dZ^2,  dZ = s Z1 + s^2 Z2  (asin's Taylor)
+// in about 40 float32 operations, with no boresight load and no table.
+// The anchor lon(ta), lat(ta) are the reference's values at ta from the
+// certified double-float pointing (fastpoint.cuh), as pixel coordinates
+// x(ta), y(ta) split into an integer and a fraction.
+//
+// Bound (ix_setup): the remainders of the two series (|z|^3 / (3(1-|z|))
+// and the asin term |dZ|^3 max|asin'''| / 6), the dropped s^3, s^4 terms
+// and the model error E through the forms' norms (|B_w(p, q)| <= |p||q|/
+// sqrt(2), |B_Z(p, q)| <= |p||q|), the float32 evaluation of the
+// coefficients and of the per-sample polynomials, the reference's table
+// interpolation error at both ends (2 x h^2/8 max|f''|) and the anchor's
+// double-float error, times a safety factor 1.5.  A sample whose pixel
+// coordinates are farther than that from every integer gets the
+// reference's pixel; the others (and every sample of a chunk whose model
+// does not apply: near the native poles, across the atan2 seam, a chunk
+// moving more than 0.05 of a radian, or one whose spin factors the model
+// would not give to 1e-7) go to the fallback pass with the double-float and
+// exact pointing.  Spin factors are float32 evaluations of the model
+// (within ~1e-7 of the reference's), as in the mixed mode's float32 tier.
+#pragma once
+
+#include "mx_common.cuh"
+
+namespace so3g {
+
+namespace {
+
+constexpr int kIxLen = 64;            // samples per chunk
+constexpr int kIxBlocksPerSM = 4;
+
+// The boresight model of one chunk.
+struct IxBore {
+    float4 d1, d2;    // Q(s) = q(ta) + s d1 + s^2 d2 (float32-rounded)
+    float e;          // max |q(t) - Q(s)| over the chunk's samples (rounded up)
+    float pad[3];
+};
+
+// Per (detector, chunk): the model's coefficients and bounds, read by every
+// lane of a warp (six 16-byte words).
+struct __align__(16) IxParams {
+    float xf, yf, c1r, c1i;     // anchor fractions; z = c1 s + c2 s^2
+    float c2r, c2i, z1, z2;     // dZ = s (z1 + s z2)
+    float k1, k2, v0r, v0i;     // dlat = dZ (k1 + k2 dZ); v = v0 + s v1 + s^2 v2
+    float v1r, v1i, v2r, v2i;
+    float bx, by, inv_len;      // bounds (pixels; 2 = chunk not modelled), 1/(tb - ta)
+    int ta;
+    int xb, yb, pad0, pad1;     // anchor integer parts
+};
+
+// The chunks' boresight models (one thread per chunk), in float64.
+__global__ void k_ix_bore(const double *bore, int n_time, int n_chunks, IxBore *out) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_chunks) return;
+    const int ta = j * kIxLen, tb = min(ta + kIxLen, n_time - 1), L = tb - ta;
+    double qa[4], d1[4], d2[4];
+    for (int k = 0; k < 4; k++) qa[k] = __ldg(bore + 4LL * ta + k);
+    if (L >= 2) {
+        const int tm = ta + L / 2;
+        const double sm = (double)(tm - ta) / L;
+        for (int k = 0; k < 4; k++) {
+            const double qm = __ldg(bore + 4LL * tm + k), qb = __ldg(bore + 4LL * tb + k);
+            d2[k] = ((qm - qa[k]) - sm * (qb - qa[k])) / (sm * sm - sm);
+            d1[k] = (qb - qa[k]) - d2[k];
+        }
+    } else {
+        for (int k = 0; k < 4; k++) {
+            d1[k] = L == 1 ? __ldg(bore + 4LL * tb + k) - qa[k] : 0.;
+            d2[k] = 0.;
+        }
+    }
+    float f1[4], f2[4];
+    for (int k = 0; k < 4; k++) {
+        f1[k] = __double2float_rn(d1[k]);
+        f2[k] = __double2float_rn(d2[k]);
+    }
+    double e = 0.;
+    for (int t = ta; t <= tb; t++) {
+        const double s = L > 0 ? (double)(t - ta) / L : 0.;
+        double n2 = 0.;
+        for (int k = 0; k < 4; k++) {
+            const double r = __ldg(bore + 4LL * t + k) - (qa[k] + s * (double)f1[k] +
+                                                          s * s * (double)f2[k]);
+            n2 += r * r;
+        }
+        e = fmax(e, sqrt(n2));
+    }
+    IxBore o;
+    o.d1 = make_float4(f1[0], f1[1], f1[2], f1[3]);
+    o.d2 = make_float4(f2[0], f2[1], f2[2], f2[3]);
+    o.e = __double2float_ru(e * (1. + 1e-6) + 1e-30);
+    o.pad[0] = o.pad[1] = o.pad[2] = 0.f;
+    out[j] = o;
+}
+
+__device__ __forceinline__ void qmul32(const float (&p)[4], const float (&q)[4], float (&r)[4]) {
+    r[0] = p[0] * q[0] - p[1] * q[1] - p[2] * q[2] - p[3] * q[3];
+    r[1] = p[0] * q[1] + p[1] * q[0] + p[2] * q[3] - p[3] * q[2];
+    r[2] = p[0] * q[2] - p[1] * q[3] + p[2] * q[0] + p[3] * q[1];
+    r[3] = p[0] * q[3] + p[1] * q[2] - p[2] * q[1] + p[3] * q[0];
+}
+
+__device__ __forceinline__ float norm4(const float (&q)[4]) {
+    return sqrtf(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+}
+
+// The three quadratic forms of (a, b, c, d) and twice their polar forms
+// B(p, q) (so that F(p + q) = F(p) + 2 B(p, q) + F(q)).
+__device__ __forceinline__ void form_w(const float (&q)[4], float &x, float &y) {
+    x = q[2] * q[0] + q[3] * q[1];
+    y = q[2] * q[3] - q[0] * q[1];
+}
+__device__ __forceinline__ void form_w2(const float (&p)[4], const float (&q)[4], float &x,
+                                        float &y) {
+    x = p[2] * q[0] + p[0] * q[2] + p[3] * q[1] + p[1] * q[3];
+    y = p[2] * q[3] + p[3] * q[2] - p[0] * q[1] - p[1] * q[0];
+}
+__device__ __forceinline__ float form_z(const float (&q)[4]) {
+    return q[0] * q[0] - q[1] * q[1] - q[2] * q[2] + q[3] * q[3];
+}
+__device__ __forceinline__ float form_z2(const float (&p)[4], const float (&q)[4]) {
+    return 2.f * (p[0] * q[0] - p[1] * q[1] - p[2] * q[2] + p[3] * q[3]);
+}
+__device__ __forceinline__ void form_v(const float (&q)[4], float &x, float &y) {
+    x = q[0] * q[2] - q[1] * q[3];
+    y = q[2] * q[3] + q[0] * q[1];
+}
+__device__ __forceinline__ void form_v2(const float (&p)[4], const float (&q)[4], float &x,
+                                        float &y) {
+    x = p[0] * q[2] + p[2] * q[0] - p[1] * q[3] - p[3] * q[1];
+    y = p[2] * q[3] + p[3] * q[2] + p[0] * q[1] + p[1] * q[0];
+}
+
+// The model of chunk j for a detector (double-float qd, float32 q32): the
+// anchor from the certified double-float pointing, the coefficients and
+// bounds as described above.  Leaves bx = by = 2 (every sample to the
+// fallback pass) where the model does not apply.
+template <class Args>
+__device__ __forceinline__ void ix_setup(const Args &a, const IxBore *ixb, int j, int n_time,
+                                         const dfl (&qd)[4], const float (&q32)[4],
+                                         IxParams &p) {
+    constexpr float u = kU;
+    const int ta = j * kIxLen, tb = min(ta + kIxLen, n_time - 1);
+    {
+        float4 *w = reinterpret_cast<float4 *>(&p);
+#pragma unroll
+        for (int k = 0; k < 6; k++) w[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    p.ta = ta;
+    p.inv_len = tb > ta ? 1.f / (float)(tb - ta) : 0.f;
+    p.bx = p.by = 2.f;
+    const double2 lo = __ldg(reinterpret_cast<const double2 *>(a.bore + 4LL * ta));
+    const double2 hi = __ldg(reinterpret_cast<const double2 *>(a.bore + 4LL * ta) + 1);
+    dfl qb[4];
+    if (!(df_split(lo.x, qb[0]) & df_split(lo.y, qb[1]) & df_split(hi.x, qb[2]) &
+          df_split(hi.y, qb[3])))
+        return;
+    dfl X, Y, Nc, Ns, D;
+    if (!fast_native<SO3G_COORD_CAR>(a.ft, a.fc, qb, qd, X, Y, Nc, Ns, D)) return;
+    const dfl xa = df_add(df_mul(X, a.fc.inv_cdx), a.fc.off_x);
+    const dfl ya = df_add(df_mul(Y, a.fc.inv_cdy), a.fc.off_y);
+    if (!(fabsf(xa.hi) < 1e7f && fabsf(ya.hi) < 1e7f)) return;
+    dfl fx, fy;
+    const int xb = df_floor(xa, fx), yb = df_floor(ya, fy);
+
+    // The model quaternions, float32.
+    const IxBore B = ixb[j];
+    const float qa[4] = {qb[0].hi, qb[1].hi, qb[2].hi, qb[3].hi};
+    const float d1[4] = {B.d1.x, B.d1.y, B.d1.z, B.d1.w};
+    const float d2[4] = {B.d2.x, B.d2.y, B.d2.z, B.d2.w};
+    float A0[4], A1[4], A2[4];
+    qmul32(qa, q32, A0);
+    qmul32(d1, q32, A1);
+    qmul32(d2, q32, A2);
+    const float n0 = norm4(A0), n1 = norm4(A1), n2 = norm4(A2);
+    // Model error through the detector rotation, with the float32 rounding
+    // of s (<= 2u s) moving the model by <= 2u (|d1| + 2 |d2|).
+    const float E = (B.e + 2.f * u * (n1 + 2.f * n2)) * 1.0001f;
+    const float Em = n0 + n1 + n2;
+    // Effect of the float32 evaluation of the coefficients (absolute, in
+    // the forms' units).
+    const float ecoef = 128.f * u * (n0 * (n1 + n2) + n1 * n1);
+
+    // Longitude: w(s) = W0 + W1 s + W2 s^2 (+ W3 s^3 + W4 s^4).
+    float w0x, w0y, w1x, w1y, w2x, w2y, t0x, t0y;
+    form_w(A0, w0x, w0y);
+    form_w2(A0, A1, w1x, w1y);
+    form_w(A1, w2x, w2y);
+    form_w2(A0, A2, t0x, t0y);
+    w2x += t0x;
+    w2y += t0y;
+    const float w0a2 = w0x * w0x + w0y * w0y;
+    const float w0a = sqrtf(w0a2);
+    if (!(w0a > 0.1f)) return;                     // |sin lat| >~ 0.98
+    const float ir = 1.f / w0a2;
+    const float c1r = (w1x * w0x + w1y * w0y) * ir, c1i = (w1y * w0x - w1x * w0y) * ir;
+    const float c2r = (w2x * w0x + w2y * w0y) * ir, c2i = (w2y * w0x - w2x * w0y) * ir;
+    const float s2 = 1.41421356f;
+    const float eta = (s2 * n1 * n2 + n2 * n2 / s2 + s2 * Em * E + E * E / s2) / w0a;
+    const float zmax = sqrtf(c1r * c1r + c1i * c1i) + sqrtf(c2r * c2r + c2i * c2i) + eta +
+                       ecoef / w0a;
+    if (!(zmax < 0.05f)) return;
+    const float dlmax = zmax * (1.f + zmax);
+    // atan2 seam: lon stays inside (-pi, pi) over the chunk.
+    if (!(fabsf(X.hi) + dlmax < 3.1405f)) return;
+    const float lon_err = zmax * zmax * zmax / (3.f * (1.f - zmax)) +
+                          eta * (1.f + 2.f * zmax) +
+                          (ecoef / w0a + 64.f * u * zmax) * (1.f + 2.f * zmax) +
+                          2.f * 3.1e-10f;
+    const float icx = fabsf(a.mc.inv_cdx), icy = fabsf(a.mc.inv_cdy);
+    const float bx = 1.5f * (lon_err * icx + 1e-7f + u * (2.f * dlmax * icx + 2.f));
+
+    // Latitude: Z(s) = Z0 + Z1 s + Z2 s^2 (+ Z3 s^3 + Z4 s^4).
+    const float Z0 = form_z(A0);
+    const float Z1 = form_z2(A0, A1);
+    const float Z2 = form_z(A1) + form_z2(A0, A2);
+    const float etaZ = 2.f * n1 * n2 + n2 * n2 + 2.f * Em * E + E * E;
+    const float dzmax = fabsf(Z1) + fabsf(Z2) + etaZ + ecoef;
+    const float Zm = fabsf(Z0) + dzmax + 1e-6f;
+    if (!(Zm < 0.95f)) return;
+    const float om = 1.f - Z0 * Z0;
+    const float k1 = rsqrtf(om), k2 = 0.5f * Z0 * k1 * k1 * k1;
+    const float omm = 1.f - Zm * Zm;
+    const float omm_r = rsqrtf(omm);
+    const float m3 = (1.f + 2.f * Zm * Zm) * omm_r * omm_r * omm_r * omm_r * omm_r;
+    const float k1m = omm_r, k2m = 0.5f * Zm * omm_r * omm_r * omm_r;
+    const float dlatmax = k1m * dzmax + k2m * dzmax * dzmax;
+    // Table interpolation error of ASIN at both ends: h^2 / 8 max|asin''|,
+    // h = 1 / (kLutN - 1).
+    const float h2_8 = 1.f / (8.f * 16383.f * 16383.f);
+    const float lat_err = dzmax * dzmax * dzmax * m3 / 6.f +
+                          (etaZ + ecoef) * (k1m + 2.f * k2m * (dzmax + etaZ + ecoef)) +
+                          64.f * u * dlatmax +
+                          2.f * (h2_8 * Zm * omm_r * omm_r * omm_r + 1e-15f);
+    const float by = 1.5f * (lat_err * icy + 1e-7f + u * (2.f * dlatmax * icy + 2.f));
+
+    // Spin: v(s) = V0 + V1 s + V2 s^2; the dropped terms and the model
+    // error must stay below 1e-7 of |v| for the float32 contract.
+    float v0x, v0y, v1x, v1y, v2x, v2y;
+    form_v(A0, v0x, v0y);
+    form_v2(A0, A1, v1x, v1y);
+    form_v(A1, v2x, v2y);
+    form_v2(A0, A2, t0x, t0y);
+    v2x += t0x;
+    v2y += t0y;
+    const float v0a = sqrtf(v0x * v0x + v0y * v0y);
+    if (!((s2 * n1 * n2 + n2 * n2 / s2 + s2 * Em * E + E * E / s2) < 1e-7f * v0a)) return;
+
+    p.xf = fx.hi + fx.lo;
+    p.yf = fy.hi + fy.lo;
+    p.xb = xb;
+    p.yb = yb;
+    p.c1r = c1r;
+    p.c1i = c1i;
+    p.c2r = c2r;
+    p.c2i = c2i;
+    p.z1 = Z1;
+    p.z2 = Z2;
+    p.k1 = k1;
+    p.k2 = k2;
+    p.v0r = v0x;
+    p.v0i = v0y;
+    p.v1r = v1x;
+    p.v1i = v1y;
+    p.v2r = v2x;
+    p.v2i = v2y;
+    p.bx = bx;
+    p.by = by;
+}
+
+// One sample of a modelled chunk: pixel (key = iy * nx + ix, on = on the
+// map) and spin factors; false when its pixel is not certified.
+__device__ __forceinline__ bool ix_eval(const IxParams &p, int t, const DGeom &g,
+                                        const MixedConst &mc, int nc, float T, float Pr,
+                                        int &key, bool &on, float *pf) {
+    const float4 *w = reinterpret_cast<const float4 *>(&p);
+    const float4 P0 = w[0], P1 = w[1], P2 = w[2], P3 = w[3], P4 = w[4], P5 = w[5];
+    const float s = (float)(t - __float_as_int(P4.w)) * P4.z;
+    const float zr = s * fmaf(s, P1.x, P0.z), zi = s * fmaf(s, P1.y, P0.w);
+    const float dl = fmaf(-zr, zi, zi);
+    const float x = fmaf(dl, mc.inv_cdx, P0.x);
+    const float dz = s * fmaf(s, P1.w, P1.z);
+    const float dlat = dz * fmaf(dz, P2.y, P2.x);
+    const float y = fmaf(dlat, mc.inv_cdy, P0.y);
+    const float fxl = floorf(x), fyl = floorf(y);
+    const float rx = x - fxl, ry = y - fyl;
+    const bool ok = rx > P4.x && rx < 1.f - P4.x && ry > P4.y && ry < 1.f - P4.y;
+    const int ix = __float_as_int(P5.x) + (int)fxl, iy = __float_as_int(P5.y) + (int)fyl;
+    on = (unsigned)ix < (unsigned)g.nx && (unsigned)iy < (unsigned)g.ny;
+    key = iy * g.nx + ix;
+    if (nc == 1) {
+        pf[0] = T;
+        pf[1] = pf[2] = 0.f;
+        return ok;
+    }
+    const float vr = fmaf(s, fmaf(s, P3.z, P3.x), P2.z);
+    const float vi = fmaf(s, fmaf(s, P3.w, P3.y), P2.w);
+    const float k = Pr * rcp_approx(fmaf(vr, vr, vi * vi));
+    const float v1 = fmaf(vr, vr, -vi * vi) * k, v2 = 2.f * vr * vi * k;
+    if (nc == 2) {
+        pf[0] = v1;
+        pf[1] = v2;
+        pf[2] = 0.f;
+    } else {
+        pf[0] = T;
+        pf[1] = v1;
+        pf[2] = v2;
+    }
+    return ok;
+}
+
+// The boresight models of a call's chunks, in stream-ordered memory; NULL
+// when the allocation fails (the caller takes the per-sample path).
+inline IxBore *ix_bore_models(const double *bore, int n_time, cudaStream_t stream) {
+    const int n_chunks = (n_time + kIxLen - 1) / kIxLen;
+    IxBore *p = nullptr;
+    if (n_chunks <= 0 ||
+        cudaMallocAsync(reinterpret_cast<void **>(&p), sizeof(IxBore) * (size_t)n_chunks,
+                        stream) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    k_ix_bore<<<(n_chunks + 127) / 128, 128, 0, stream>>>(bore, n_time, n_chunks, p);
+    if (after_launch("boresight chunk models") != SO3G_OK) {
+        cudaFreeAsync(p, stream);
+        clear_error();
+        return nullptr;
+    }
+    return p;
+}
+
+}  // namespace
+
+}  // namespace so3g

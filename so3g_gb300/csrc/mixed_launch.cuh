@@ -22,6 +22,7 @@
 #pragma once
 
 #include "mx_common.cuh"
+#include "interp_point.cuh"
 #include "scatter_kernel.cuh"
 
 namespace so3g {
@@ -154,6 +155,143 @@ __global__ void __launch_bounds__(kBlock) k_scatter_mx_fix(ScatterArgs a, MxMask
     });
 }
 
+// The chunked main pass for CAR maps (interp_point.cuh).  Block (x, y):
+// piece y of detector x; warp w models the groups of 32 chunks g = w, w + 8,
+// ... of the piece (one chunk per lane, parameters in shared memory), then
+// walks their samples 32 at a time (lane = sample).  Samples it cannot
+// certify are marked in the mask as in k_scatter_mx.
+template <bool WEIGHT>
+__global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
+    k_scatter_ix(ScatterArgs a, MxMask mm, const IxBore *ixb) {
+    __shared__ IxParams sp[kBlock / 32][32];
+    int det, t0, t1;
+    if (!seg_piece(a.segs, a.piece, det, t0, t1)) return;
+    float det_wt = 1.f;
+    if (a.det_weights) {
+        det_wt = __ldg(a.det_weights + det);
+        if (det_wt == 0.f) return;  // src/Projection.cxx:1784-1788
+    }
+    const QuatD ofs = load_quat(a.dets + 4LL * det);
+    const dfl qd[4] = {df_of(ofs.a), df_of(ofs.b), df_of(ofs.c), df_of(ofs.d)};
+    const float q32[4] = {d2f_round(ofs.a), d2f_round(ofs.b), d2f_round(ofs.c),
+                          d2f_round(ofs.d)};
+    const float T = __ldg(a.resp + 2 * det), Pr = __ldg(a.resp + 2 * det + 1);
+    const int nc = a.g.ncomp;
+    constexpr int NV = WEIGHT ? 6 : 3;
+    int mult[NV];
+    const unsigned vmask = value_slots<WEIGHT>(nc, mult);
+    const long long plane = (long long)a.g.ny * a.g.nx;
+    const float *sig = a.signal + det * a.sig_stride;
+    unsigned *mwb = mm.words + ((long long)blockIdx.x * gridDim.y + blockIdx.y) * mm.wpp;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int j0 = t0 / kIxLen, j1 = (t1 - 1) / kIxLen + 1;
+    for (int g = j0 + warp * 32; g < j1; g += (kBlock / 32) * 32) {
+        if (g + lane < j1) ix_setup(a, ixb, g + lane, a.segs.n_time, qd, q32, sp[warp][lane]);
+        __syncwarp();
+        const int nch = min(32, j1 - g);
+        for (int k = 0; k < nch; k++) {
+#pragma unroll
+            for (int h = 0; h < kIxLen / 32; h++) {
+                const int tw = (g + k) * kIxLen + h * 32;
+                const int t = tw + lane;
+                const bool live = t >= t0 && t < t1;
+                const float s_in = (!WEIGHT && live) ? __ldg(sig + t) : 0.f;
+                int key = 0;
+                bool on = false;
+                float pf[3];
+                const bool ok = ix_eval(sp[warp][k], t, a.g, a.mc, nc, T, Pr, key, on, pf) &&
+                                live;
+                const unsigned fails = __ballot_sync(kFull, live && !ok);
+                if (fails && lane == 0) mwb[(tw - t0) / 32] = fails;
+                if (!(ok && on)) key = -1;
+                float v[NV];
+                tap_values<WEIGHT, NV, true>(s_in, pf, 1.f, det_wt, v);
+                if (a.accum == SO3G_ACCUM_WARP_RUNS) {
+                    flush_runs32<NV, kDirectRuns>(key, plane, v, mult, vmask, a.map);
+                } else if (key >= 0) {
+                    double *p = a.map + key;
+#pragma unroll
+                    for (int q = 0; q < NV; q++)
+                        if ((vmask >> q) & 1u) atomicAdd(p + mult[q] * plane, f2d(v[q]));
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// The fallback pass of k_scatter_ix: the float32 tier, then the
+// double-float pointing (float32 spin factors and terms), then the exact
+// float64 pointing.
+template <bool WEIGHT>
+__global__ void __launch_bounds__(kBlock) k_scatter_ix_fix(ScatterArgs a, MxMask mm) {
+    constexpr int C = SO3G_COORD_CAR, P = PX_FLAT_NT_NN;
+    constexpr int NV = WEIGHT ? 6 : 3;
+    int mult[NV];
+    const int nc = a.g.ncomp;
+    const unsigned vmask = value_slots<WEIGHT>(nc, mult);
+    const long long plane = (long long)a.g.ny * a.g.nx;
+    mx_for_each(a.segs, a.piece, mm, [&](int det, int t) {
+        const float det_wt = a.det_weights ? __ldg(a.det_weights + det) : 1.f;
+        const QuatD ofs = load_quat(a.dets + 4LL * det);
+        const float T = __ldg(a.resp + 2 * det), Pr = __ldg(a.resp + 2 * det + 1);
+        const float q32[4] = {d2f_round(ofs.a), d2f_round(ofs.b), d2f_round(ofs.c),
+                              d2f_round(ofs.d)};
+        float qb[4];
+        load_bore_f32(a.bore32, a.bore, t, qb);
+        int pix[2];
+        float pf[3] = {0.f, 0.f, 0.f};
+        bool on = false;
+        if (mixed_pointing<C, P, true, false>(a.g, a.ft, a.mc, qb, q32, nc, T, Pr, pix, on,
+                                              pf)) {
+            if (on) {
+                const float sg = WEIGHT ? 0.f : __ldg(a.signal + det * a.sig_stride + t);
+                float v[NV];
+                tap_values<WEIGHT, NV, true>(sg, pf, 1.f, det_wt, v);
+                double *p = a.map + (pix[0] * a.g.nx + pix[1]);
+#pragma unroll
+                for (int q = 0; q < NV; q++)
+                    if ((vmask >> q) & 1u) atomicAdd(p + mult[q] * plane, f2d(v[q]));
+            }
+            return;
+        }
+        const dfl qd[4] = {df_of(ofs.a), df_of(ofs.b), df_of(ofs.c), df_of(ofs.d)};
+        if (!df_sample<C, P, WEIGHT, false>(a, det, t, qd, T, Pr, det_wt, mult, vmask))
+            exact_sample<C, P, WEIGHT>(a, det, t, ofs, T, Pr, det_wt, mult, vmask);
+    });
+}
+
+// The chunked pointing for CAR maps with the untiled nearest-neighbour
+// pixelizor over whole detectors (no sample segments); returns 1 (nothing
+// launched) where it does not apply or an allocation fails.
+template <int C, int P, bool WEIGHT>
+int scatter_interp(const ScatterArgs &a, dim3 grid, cudaStream_t stream) {
+    if constexpr (!(C == SO3G_COORD_CAR && P == PX_FLAT_NT_NN)) {
+        return 1;
+    } else {
+        const long long npix = (long long)a.g.ny * a.g.nx;
+        if (a.segs.seg || a.segs.n_time < 2 || npix >= (1LL << 31) || a.piece % kIxLen)
+            return 1;
+        IxBore *ixb = ix_bore_models(a.bore, a.segs.n_time, stream);
+        if (!ixb) return 1;
+        MxMask mm;
+        if (!mx_mask_alloc(mm, grid, a.piece, stream)) {
+            cudaFreeAsync(ixb, stream);
+            return 1;
+        }
+        k_scatter_ix<WEIGHT><<<grid, kBlock, 0, stream>>>(a, mm, ixb);
+        int rc = after_launch(WEIGHT ? "to_weight_map (chunked)" : "to_map (chunked)");
+        if (rc == SO3G_OK) {
+            k_scatter_ix_fix<WEIGHT><<<mx_fix_blocks(mm), kBlock, 0, stream>>>(a, mm);
+            rc = after_launch(WEIGHT ? "to_weight_map (chunked fallback)"
+                                     : "to_map (chunked fallback)");
+        }
+        cudaFreeAsync(mm.words, stream);
+        cudaFreeAsync(ixb, stream);
+        return rc;
+    }
+}
+
 // Runs the two passes on a.segs / grid; returns 1 (nothing launched, the
 // caller runs k_scatter) when the pixelization is not eligible, the map
 // index does not fit 31 bits, or the mask cannot be allocated.
@@ -162,6 +300,8 @@ int scatter_mixed(const ScatterArgs &a, dim3 grid, cudaStream_t stream) {
     if constexpr (!MxEligible<C, P>::value) {
         return 1;
     } else {
+        const int ri = scatter_interp<C, P, WEIGHT>(a, grid, stream);
+        if (ri != 1) return ri;
         const long long npix = P == PX_HP_NT ? a.g.npix : (long long)a.g.ny * a.g.nx;
         if (!a.bore32 || npix >= (1LL << 31)) return 1;
         MxMask mm;
