@@ -517,17 +517,33 @@ __global__ void __launch_bounds__(kBlock, kMxBlocksPerSM) k_from_map_mx(GatherAr
     }
 }
 
-// Fallback pass of k_from_map_mx: double-float pointing (float32 spin
-// factors and terms), then the exact float64 pointing.
-template <int C, int P>
+// Fallback passes of k_from_map_mx, by tier: 1 the double-float pointing
+// (float32 spin factors and terms), 2 the exact float64 pointing for the
+// samples tier 1 could not certify.
+template <int C, int P, int TIER>
 __global__ void __launch_bounds__(kBlock) k_from_map_mx_fix(GatherArgs a, MxMask mm) {
-    mx_for_each(a.segs, a.piece, mm, [&](int det, int t) {
+    mx_for_each<TIER == 1>(a.segs, a.piece, mm, [&](int det, int t) -> bool {
         const QuatD ofs = load_quat(a.dets + 4LL * det);
-        const dfl qd[4] = {df_of(ofs.a), df_of(ofs.b), df_of(ofs.c), df_of(ofs.d)};
         const float T = __ldg(a.resp + 2 * det), Pr = __ldg(a.resp + 2 * det + 1);
-        if (!df_gather<C, P>(a, det, t, qd, T, Pr)) exact_gather<C, P>(a, det, t, ofs, T, Pr);
+        if constexpr (TIER == 1) {
+            const dfl qd[4] = {df_of(ofs.a), df_of(ofs.b), df_of(ofs.c), df_of(ofs.d)};
+            return df_gather<C, P>(a, det, t, qd, T, Pr);
+        } else {
+            exact_gather<C, P>(a, det, t, ofs, T, Pr);
+            return true;
+        }
     });
 }
+
+template <int C, int P>
+struct GatherMxFix {
+    const GatherArgs &a;
+    const MxMask &mm;
+    template <int T>
+    void launch(unsigned nb, cudaStream_t st) const {
+        if constexpr (T > 0) k_from_map_mx_fix<C, P, T><<<nb, kBlock, 0, st>>>(a, mm);
+    }
+};
 
 // The chunked from_map for CAR maps (interp_point.cuh), laid out as
 // k_scatter_ix: the map read from its float32 copy, the signal updated
@@ -580,23 +596,27 @@ __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
     }
 }
 
-// Fallback pass of k_from_map_ix: the float32 tier, then the double-float
-// pointing (float32 spin factors and terms), then the exact float64 one.
+// Fallback passes of k_from_map_ix, by tier: 0 the float32 tier, 1 the
+// double-float pointing (float32 spin factors and terms), 2 the exact
+// float64 pointing, each on the samples the previous tier left.
+template <int TIER>
 __global__ void __launch_bounds__(kBlock) k_from_map_ix_fix(GatherArgs a, MxMask mm) {
     constexpr int C = SO3G_COORD_CAR, P = PX_FLAT_NT_NN;
     const int nc = a.g.ncomp;
-    mx_for_each(a.segs, a.piece, mm, [&](int det, int t) {
+    mx_for_each<TIER < 2>(a.segs, a.piece, mm, [&](int det, int t) -> bool {
         const QuatD ofs = load_quat(a.dets + 4LL * det);
         const float T = __ldg(a.resp + 2 * det), Pr = __ldg(a.resp + 2 * det + 1);
-        const float q32[4] = {d2f_round(ofs.a), d2f_round(ofs.b), d2f_round(ofs.c),
-                              d2f_round(ofs.d)};
-        float qb[4];
-        load_bore_f32(a.bore32, a.bore, t, qb);
-        int pix[2];
-        float pf[3] = {0.f, 0.f, 0.f};
-        bool on = false;
-        if (mixed_pointing<C, P, true, false>(a.g, a.ft, a.mc, qb, q32, nc, T, Pr, pix, on,
-                                              pf)) {
+        if constexpr (TIER == 0) {
+            const float q32[4] = {d2f_round(ofs.a), d2f_round(ofs.b), d2f_round(ofs.c),
+                                  d2f_round(ofs.d)};
+            float qb[4];
+            load_bore_f32(a.bore32, a.bore, t, qb);
+            int pix[2];
+            float pf[3] = {0.f, 0.f, 0.f};
+            bool on = false;
+            if (!mixed_pointing<C, P, true, false>(a.g, a.ft, a.mc, qb, q32, nc, T, Pr, pix, on,
+                                                   pf))
+                return false;
             if (on) {
                 float *sp = a.signal + det * a.sig_stride + t;
                 const float4 m = __ldg(a.map32 + (pix[0] * a.g.nx + pix[1]));
@@ -605,12 +625,25 @@ __global__ void __launch_bounds__(kBlock) k_from_map_ix_fix(GatherArgs a, MxMask
                 if (nc > 2) sv = fmaf(m.z, pf[2], sv);
                 *sp = sv;
             }
-            return;
+            return true;
+        } else if constexpr (TIER == 1) {
+            const dfl qd[4] = {df_of(ofs.a), df_of(ofs.b), df_of(ofs.c), df_of(ofs.d)};
+            return df_gather<C, P>(a, det, t, qd, T, Pr);
+        } else {
+            exact_gather<C, P>(a, det, t, ofs, T, Pr);
+            return true;
         }
-        const dfl qd[4] = {df_of(ofs.a), df_of(ofs.b), df_of(ofs.c), df_of(ofs.d)};
-        if (!df_gather<C, P>(a, det, t, qd, T, Pr)) exact_gather<C, P>(a, det, t, ofs, T, Pr);
     });
 }
+
+struct GatherIxFix {
+    const GatherArgs &a;
+    const MxMask &mm;
+    template <int T>
+    void launch(unsigned nb, cudaStream_t st) const {
+        k_from_map_ix_fix<T><<<nb, kBlock, 0, st>>>(a, mm);
+    }
+};
 
 // The chunked from_map for CAR maps with the untiled nearest-neighbour
 // pixelizor; returns 1 (nothing launched) where it does not apply.
@@ -632,10 +665,7 @@ int gather_interp(const GatherArgs &a, dim3 grid, cudaStream_t stream) {
         }
         k_from_map_ix<<<grid, kBlock, 0, stream>>>(a, mm, ixb);
         int rc = after_launch("from_map (chunked)");
-        if (rc == SO3G_OK) {
-            k_from_map_ix_fix<<<mx_fix_blocks(mm), kBlock, 0, stream>>>(a, mm);
-            rc = after_launch("from_map (chunked fallback)");
-        }
+        if (rc == SO3G_OK) rc = fix_tiers<0>(GatherIxFix{a, mm}, mm, stream, "from_map (chunked fallback)");
         cudaFreeAsync(mm.words, stream);
         cudaFreeAsync(ixb, stream);
         return rc;
@@ -659,10 +689,8 @@ int gather_mixed(const GatherArgs &a, dim3 grid, cudaStream_t stream) {
         if (!mx_mask_alloc(mm, grid, a.piece, stream)) return 1;
         k_from_map_mx<C, P><<<grid, kBlock, 0, stream>>>(a, mm);
         int rc = after_launch("from_map (mixed)");
-        if (rc == SO3G_OK) {
-            k_from_map_mx_fix<C, P><<<mx_fix_blocks(mm), kBlock, 0, stream>>>(a, mm);
-            rc = after_launch("from_map (mixed fallback)");
-        }
+        if (rc == SO3G_OK)
+            rc = fix_tiers<1>(GatherMxFix<C, P>{a, mm}, mm, stream, "from_map (mixed fallback)");
         cudaFreeAsync(mm.words, stream);
         return rc;
     }

@@ -16,15 +16,16 @@
 // so along the model each is a polynomial in s, of degree 4 with its s^3
 // and s^4 coefficients negligible (|A2| ~ 1e-6): per sample,
 //   lon = lon(ta) + arg(1 + z),  z = c1 s + c2 s^2 (c_k = W_k / W_0)
-//         ~ lon(ta) + Im z - Re z Im z                   (|z| < 0.05)
-//   lat = lat(ta) + k1 dZ + k2 dZ^2,  dZ = s Z1 + s^2 Z2  (asin's Taylor)
+//         ~ lon(ta) + Im(z - z^2/2 + z^3/3)              (|z| < 0.05)
+//   lat = lat(ta) + k1 dZ + k2 dZ^2 + k3 dZ^3,  dZ = s Z1 + s^2 Z2
+//         (asin's Taylor series)
 // in about 40 float32 operations, with no boresight load and no table.
 // The anchor lon(ta), lat(ta) are the reference's values at ta from the
 // certified double-float pointing (fastpoint.cuh), as pixel coordinates
 // x(ta), y(ta) split into an integer and a fraction.
 //
-// Bound (ix_setup): the remainders of the two series (|z|^3 / (3(1-|z|))
-// and the asin term |dZ|^3 max|asin'''| / 6), the dropped s^3, s^4 terms
+// Bound (ix_setup): the remainders of the two series (|z|^4 / (4(1-|z|))
+// and the asin term |dZ|^4 max|asin''''| / 24), the dropped s^3, s^4 terms
 // and the model error E through the forms' norms (|B_w(p, q)| <= |p||q|/
 // sqrt(2), |B_Z(p, q)| <= |p||q|), the float32 evaluation of the
 // coefficients and of the per-sample polynomials, the reference's table
@@ -64,7 +65,8 @@ struct __align__(16) IxParams {
     float v1r, v1i, v2r, v2i;
     float bx, by, inv_len;      // bounds (pixels; 2 = chunk not modelled), 1/(tb - ta)
     int ta;
-    int xb, yb, pad0, pad1;     // anchor integer parts
+    int xb, yb;                 // anchor integer parts
+    float k3, pad0;             // dlat's cubic coefficient
 };
 
 // The chunks' boresight models (one thread per chunk), in float64.
@@ -197,8 +199,18 @@ __device__ __forceinline__ void ix_setup(const Args &a, const IxBore *ixb, int j
     const float E = (B.e + 2.f * u * (n1 + 2.f * n2)) * 1.0001f;
     const float Em = n0 + n1 + n2;
     // Effect of the float32 evaluation of the coefficients (absolute, in
-    // the forms' units).
-    const float ecoef = 128.f * u * (n0 * (n1 + n2) + n1 * n1);
+    // the forms' units).  A0 is within 10u n0 of q(ta) (x) q_d (2u from
+    // rounding both factors, 2 gamma_4 from the product's four-term sums),
+    // A1 and A2 within 9u of their norms (d1, d2 are the model's own).
+    // Through the polar forms (|2B_w| <= sqrt2, |2B_Z| <= 2) and their
+    // four-term sums: W1 within 33u n0 n1, W2 within 34u n0 n2 + 17u n1^2,
+    // Z1 within 46u n0 n1, Z2 within 47u n0 n2 + 23u n1^2.
+    const float ecoef = 48.f * u * (n0 * (n1 + n2) + n1 * n1);
+    // W0 and Z0 are evaluated from A0: W0 to 17u n0^2 (relative 17u n0^2 /
+    // |W0| once divided out), Z0 to 24u n0^2 (moving the asin
+    // coefficients).
+    const float rel0 = 17.f * u * n0 * n0;
+    const float dZ0 = 24.f * u * n0 * n0;
 
     // Longitude: w(s) = W0 + W1 s + W2 s^2 (+ W3 s^3 + W4 s^4).
     float w0x, w0y, w1x, w1y, w2x, w2y, t0x, t0y;
@@ -222,9 +234,14 @@ __device__ __forceinline__ void ix_setup(const Args &a, const IxBore *ixb, int j
     const float dlmax = zmax * (1.f + zmax);
     // atan2 seam: lon stays inside (-pi, pi) over the chunk.
     if (!(fabsf(X.hi) + dlmax < 3.1405f)) return;
-    const float lon_err = zmax * zmax * zmax / (3.f * (1.f - zmax)) +
-                          eta * (1.f + 2.f * zmax) +
-                          (ecoef / w0a + 64.f * u * zmax) * (1.f + 2.f * zmax) +
+    // Series remainder, the dropped terms (eta) and the coefficients'
+    // errors through the series' derivative (<= 1 + 2|z|): W1, W2's
+    // absolute errors, W0's relative error, the division's roundings (6u
+    // |c|) and the per-sample evaluation (6u |z|); and the ATAN2 table's
+    // interpolation error at both ends (h^2/8 max|atan''| = 3.0e-10).
+    const float z2m = zmax * zmax;
+    const float lon_err = z2m * z2m / (4.f * (1.f - zmax)) + eta * (1.f + 2.f * zmax) +
+                          (ecoef / w0a + (rel0 / w0a + 12.f * u) * zmax) * (1.f + 2.f * zmax) +
                           2.f * 3.1e-10f;
     const float icx = fabsf(a.mc.inv_cdx), icy = fabsf(a.mc.inv_cdy);
     const float bx = 1.5f * (lon_err * icx + 1e-7f + u * (2.f * dlmax * icx + 2.f));
@@ -237,20 +254,31 @@ __device__ __forceinline__ void ix_setup(const Args &a, const IxBore *ixb, int j
     const float dzmax = fabsf(Z1) + fabsf(Z2) + etaZ + ecoef;
     const float Zm = fabsf(Z0) + dzmax + 1e-6f;
     if (!(Zm < 0.95f)) return;
+    // asin's Taylor coefficients at Z0: asin' = (1-Z^2)^-1/2, asin'' =
+    // Z (1-Z^2)^-3/2, asin''' = (1+2Z^2)(1-Z^2)^-5/2, asin'''' = Z (9+6Z^2)
+    // (1-Z^2)^-7/2, all increasing in |Z|; their bounds at Zm.
     const float om = 1.f - Z0 * Z0;
-    const float k1 = rsqrtf(om), k2 = 0.5f * Z0 * k1 * k1 * k1;
+    const float k1 = rsqrtf(om), k1c = k1 * k1 * k1;
+    const float k2 = 0.5f * Z0 * k1c;
+    const float k3 = (1.f + 2.f * Z0 * Z0) * k1c * k1 * k1 * (1.f / 6.f);
     const float omm = 1.f - Zm * Zm;
-    const float omm_r = rsqrtf(omm);
-    const float m3 = (1.f + 2.f * Zm * Zm) * omm_r * omm_r * omm_r * omm_r * omm_r;
-    const float k1m = omm_r, k2m = 0.5f * Zm * omm_r * omm_r * omm_r;
-    const float dlatmax = k1m * dzmax + k2m * dzmax * dzmax;
+    const float r = rsqrtf(omm), r3 = r * r * r, r5 = r3 * r * r;
+    const float m4 = Zm * (9.f + 6.f * Zm * Zm) * r5 * r * r;
+    const float k1m = r, k2m = 0.5f * Zm * r3, k3m = (1.f + 2.f * Zm * Zm) * r5 * (1.f / 6.f);
+    const float dzm = dzmax + etaZ + ecoef;
+    const float dlatmax = dzmax * (k1m + dzmax * (k2m + dzmax * k3m));
     // Table interpolation error of ASIN at both ends: h^2 / 8 max|asin''|,
     // h = 1 / (kLutN - 1).
     const float h2_8 = 1.f / (8.f * 16383.f * 16383.f);
-    const float lat_err = dzmax * dzmax * dzmax * m3 / 6.f +
-                          (etaZ + ecoef) * (k1m + 2.f * k2m * (dzmax + etaZ + ecoef)) +
-                          64.f * u * dlatmax +
-                          2.f * (h2_8 * Zm * omm_r * omm_r * omm_r + 1e-15f);
+    const float dz2 = dzmax * dzmax;
+    // Series remainder; dZ's errors through the series' derivative; Z0's
+    // error through the coefficients (d k_n / dZ0 = (n + 1) k_(n+1)); the
+    // roundings of the coefficients and of the per-sample evaluation
+    // (32u |dlat|); the ASIN table at both ends and the anchor.
+    const float lat_err = dz2 * dz2 * m4 / 24.f +
+                          (etaZ + ecoef) * (k1m + 2.f * k2m * dzm + 3.f * k3m * dzm * dzm) +
+                          dZ0 * dzm * (2.f * k2m + dzm * (3.f * k3m + dzm * m4 / 6.f)) +
+                          32.f * u * dlatmax + 2.f * (h2_8 * Zm * r3 + 1e-15f);
     const float by = 1.5f * (lat_err * icy + 1e-7f + u * (2.f * dlatmax * icy + 2.f));
 
     // Spin: v(s) = V0 + V1 s + V2 s^2; the dropped terms and the model
@@ -277,6 +305,7 @@ __device__ __forceinline__ void ix_setup(const Args &a, const IxBore *ixb, int j
     p.z2 = Z2;
     p.k1 = k1;
     p.k2 = k2;
+    p.k3 = k3;
     p.v0r = v0x;
     p.v0i = v0y;
     p.v1r = v1x;
@@ -296,10 +325,11 @@ __device__ __forceinline__ bool ix_eval(const IxParams &p, int t, const DGeom &g
     const float4 P0 = w[0], P1 = w[1], P2 = w[2], P3 = w[3], P4 = w[4], P5 = w[5];
     const float s = (float)(t - __float_as_int(P4.w)) * P4.z;
     const float zr = s * fmaf(s, P1.x, P0.z), zi = s * fmaf(s, P1.y, P0.w);
-    const float dl = fmaf(-zr, zi, zi);
+    // Im(z - z^2/2 + z^3/3) = zi (1 - zr + zr^2 - zi^2/3)
+    const float dl = zi * fmaf(-0.33333334f * zi, zi, fmaf(zr, zr - 1.f, 1.f));
     const float x = fmaf(dl, mc.inv_cdx, P0.x);
     const float dz = s * fmaf(s, P1.w, P1.z);
-    const float dlat = dz * fmaf(dz, P2.y, P2.x);
+    const float dlat = dz * fmaf(dz, fmaf(dz, P5.z, P2.y), P2.x);
     const float y = fmaf(dlat, mc.inv_cdy, P0.y);
     const float fxl = floorf(x), fyl = floorf(y);
     const float rx = x - fxl, ry = y - fyl;

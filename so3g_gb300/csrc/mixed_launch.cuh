@@ -138,20 +138,25 @@ __global__ void __launch_bounds__(kBlock, kMxBlocksPerSM) k_scatter_mx(ScatterAr
     }
 }
 
-// The fallback pass of k_scatter_mx: double-float pointing (float32 spin
-// factors and terms), then the exact float64 pointing.
-template <int C, int P, bool WEIGHT>
+// The fallback passes of k_scatter_mx, by tier: 1 the double-float
+// pointing (float32 spin factors and terms), 2 the exact float64 pointing
+// for the samples tier 1 could not certify.
+template <int C, int P, bool WEIGHT, int TIER>
 __global__ void __launch_bounds__(kBlock) k_scatter_mx_fix(ScatterArgs a, MxMask mm) {
     constexpr int NV = WEIGHT ? 6 : 3;
     int mult[NV];
     const unsigned vmask = value_slots<WEIGHT>(a.g.ncomp, mult);
-    mx_for_each(a.segs, a.piece, mm, [&](int det, int t) {
+    mx_for_each<TIER == 1>(a.segs, a.piece, mm, [&](int det, int t) -> bool {
         const float det_wt = a.det_weights ? __ldg(a.det_weights + det) : 1.f;
         const QuatD ofs = load_quat(a.dets + 4LL * det);
-        const dfl qd[4] = {df_of(ofs.a), df_of(ofs.b), df_of(ofs.c), df_of(ofs.d)};
         const float T = __ldg(a.resp + 2 * det), Pr = __ldg(a.resp + 2 * det + 1);
-        if (!df_sample<C, P, WEIGHT, false>(a, det, t, qd, T, Pr, det_wt, mult, vmask))
+        if constexpr (TIER == 1) {
+            const dfl qd[4] = {df_of(ofs.a), df_of(ofs.b), df_of(ofs.c), df_of(ofs.d)};
+            return df_sample<C, P, WEIGHT, false>(a, det, t, qd, T, Pr, det_wt, mult, vmask);
+        } else {
             exact_sample<C, P, WEIGHT>(a, det, t, ofs, T, Pr, det_wt, mult, vmask);
+            return true;
+        }
     });
 }
 
@@ -220,10 +225,10 @@ __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
     }
 }
 
-// The fallback pass of k_scatter_ix: the float32 tier, then the
-// double-float pointing (float32 spin factors and terms), then the exact
-// float64 pointing.
-template <bool WEIGHT>
+// The fallback passes of k_scatter_ix, by tier: 0 the float32 tier, 1 the
+// double-float pointing (float32 spin factors and terms), 2 the exact
+// float64 pointing, each on the samples the previous tier left.
+template <bool WEIGHT, int TIER>
 __global__ void __launch_bounds__(kBlock) k_scatter_ix_fix(ScatterArgs a, MxMask mm) {
     constexpr int C = SO3G_COORD_CAR, P = PX_FLAT_NT_NN;
     constexpr int NV = WEIGHT ? 6 : 3;
@@ -231,19 +236,21 @@ __global__ void __launch_bounds__(kBlock) k_scatter_ix_fix(ScatterArgs a, MxMask
     const int nc = a.g.ncomp;
     const unsigned vmask = value_slots<WEIGHT>(nc, mult);
     const long long plane = (long long)a.g.ny * a.g.nx;
-    mx_for_each(a.segs, a.piece, mm, [&](int det, int t) {
+    mx_for_each<TIER < 2>(a.segs, a.piece, mm, [&](int det, int t) -> bool {
         const float det_wt = a.det_weights ? __ldg(a.det_weights + det) : 1.f;
         const QuatD ofs = load_quat(a.dets + 4LL * det);
         const float T = __ldg(a.resp + 2 * det), Pr = __ldg(a.resp + 2 * det + 1);
-        const float q32[4] = {d2f_round(ofs.a), d2f_round(ofs.b), d2f_round(ofs.c),
-                              d2f_round(ofs.d)};
-        float qb[4];
-        load_bore_f32(a.bore32, a.bore, t, qb);
-        int pix[2];
-        float pf[3] = {0.f, 0.f, 0.f};
-        bool on = false;
-        if (mixed_pointing<C, P, true, false>(a.g, a.ft, a.mc, qb, q32, nc, T, Pr, pix, on,
-                                              pf)) {
+        if constexpr (TIER == 0) {
+            const float q32[4] = {d2f_round(ofs.a), d2f_round(ofs.b), d2f_round(ofs.c),
+                                  d2f_round(ofs.d)};
+            float qb[4];
+            load_bore_f32(a.bore32, a.bore, t, qb);
+            int pix[2];
+            float pf[3] = {0.f, 0.f, 0.f};
+            bool on = false;
+            if (!mixed_pointing<C, P, true, false>(a.g, a.ft, a.mc, qb, q32, nc, T, Pr, pix, on,
+                                                   pf))
+                return false;
             if (on) {
                 const float sg = WEIGHT ? 0.f : __ldg(a.signal + det * a.sig_stride + t);
                 float v[NV];
@@ -253,13 +260,36 @@ __global__ void __launch_bounds__(kBlock) k_scatter_ix_fix(ScatterArgs a, MxMask
                 for (int q = 0; q < NV; q++)
                     if ((vmask >> q) & 1u) atomicAdd(p + mult[q] * plane, f2d(v[q]));
             }
-            return;
-        }
-        const dfl qd[4] = {df_of(ofs.a), df_of(ofs.b), df_of(ofs.c), df_of(ofs.d)};
-        if (!df_sample<C, P, WEIGHT, false>(a, det, t, qd, T, Pr, det_wt, mult, vmask))
+            return true;
+        } else if constexpr (TIER == 1) {
+            const dfl qd[4] = {df_of(ofs.a), df_of(ofs.b), df_of(ofs.c), df_of(ofs.d)};
+            return df_sample<C, P, WEIGHT, false>(a, det, t, qd, T, Pr, det_wt, mult, vmask);
+        } else {
             exact_sample<C, P, WEIGHT>(a, det, t, ofs, T, Pr, det_wt, mult, vmask);
+            return true;
+        }
     });
 }
+
+template <bool WEIGHT>
+struct ScatterIxFix {
+    const ScatterArgs &a;
+    const MxMask &mm;
+    template <int T>
+    void launch(unsigned nb, cudaStream_t st) const {
+        k_scatter_ix_fix<WEIGHT, T><<<nb, kBlock, 0, st>>>(a, mm);
+    }
+};
+
+template <int C, int P, bool WEIGHT>
+struct ScatterMxFix {
+    const ScatterArgs &a;
+    const MxMask &mm;
+    template <int T>
+    void launch(unsigned nb, cudaStream_t st) const {
+        if constexpr (T > 0) k_scatter_mx_fix<C, P, WEIGHT, T><<<nb, kBlock, 0, st>>>(a, mm);
+    }
+};
 
 // The chunked pointing for CAR maps with the untiled nearest-neighbour
 // pixelizor over whole detectors (no sample segments); returns 1 (nothing
@@ -281,11 +311,10 @@ int scatter_interp(const ScatterArgs &a, dim3 grid, cudaStream_t stream) {
         }
         k_scatter_ix<WEIGHT><<<grid, kBlock, 0, stream>>>(a, mm, ixb);
         int rc = after_launch(WEIGHT ? "to_weight_map (chunked)" : "to_map (chunked)");
-        if (rc == SO3G_OK) {
-            k_scatter_ix_fix<WEIGHT><<<mx_fix_blocks(mm), kBlock, 0, stream>>>(a, mm);
-            rc = after_launch(WEIGHT ? "to_weight_map (chunked fallback)"
+        if (rc == SO3G_OK)
+            rc = fix_tiers<0>(ScatterIxFix<WEIGHT>{a, mm}, mm, stream,
+                              WEIGHT ? "to_weight_map (chunked fallback)"
                                      : "to_map (chunked fallback)");
-        }
         cudaFreeAsync(mm.words, stream);
         cudaFreeAsync(ixb, stream);
         return rc;
@@ -308,11 +337,10 @@ int scatter_mixed(const ScatterArgs &a, dim3 grid, cudaStream_t stream) {
         if (!mx_mask_alloc(mm, grid, a.piece, stream)) return 1;
         k_scatter_mx<C, P, WEIGHT><<<grid, kBlock, 0, stream>>>(a, mm);
         int rc = after_launch(WEIGHT ? "to_weight_map (mixed)" : "to_map (mixed)");
-        if (rc == SO3G_OK) {
-            k_scatter_mx_fix<C, P, WEIGHT><<<mx_fix_blocks(mm), kBlock, 0, stream>>>(a, mm);
-            rc = after_launch(WEIGHT ? "to_weight_map (mixed fallback)"
+        if (rc == SO3G_OK)
+            rc = fix_tiers<1>(ScatterMxFix<C, P, WEIGHT>{a, mm}, mm, stream,
+                              WEIGHT ? "to_weight_map (mixed fallback)"
                                      : "to_map (mixed fallback)");
-        }
         cudaFreeAsync(mm.words, stream);
         return rc;
     }

@@ -4,9 +4,11 @@
 //
 // The main pass handles one sample per lane in rounds of kBlock samples;
 // each warp records the samples its float32 tier could not certify as one
-// 32-bit word per round (bit b = lane b).  The fallback pass visits the set
-// bits (mx_for_each), 32 mask words per warp, dealing the bits out to the
-// lanes by prefix sum so that every lane has a sample to work on.
+// 32-bit word per round (bit b = lane b).  The fallback passes, one per
+// tier of pointing, visit the set bits (mx_for_each), 32 mask words per
+// warp, dealing the bits out to the lanes by prefix sum so that every lane
+// has a sample to work on, and leave in the mask the samples that the next
+// tier must take.
 #pragma once
 
 #include "host.h"
@@ -34,11 +36,25 @@ struct MxMask {
     int gy;          // pieces per segment (grid.y of the main kernel)
 };
 
-// Position of the k-th (0-based) set bit of w (w has more than k set bits).
+// Position of the k-th (0-based) set bit of w (w has more than k set bits),
+// by bisection on the bit counts of the lower halves.
 __device__ __forceinline__ int nth_bit(unsigned w, int k) {
-    for (int i = 0; i < k; i++) w &= w - 1u;
-    return __ffs(w) - 1;
+    int pos = 0;
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+        const int c = __popc(w & ((1u << s) - 1u));
+        if (k >= c) {
+            k -= c;
+            w >>= s;
+            pos += s;
+        }
+    }
+    return pos;
 }
+
+// Mask words per lane in one window of mx_for_each (a warp reads 32 x this
+// many words at once).
+constexpr int kMxWin = 8;
 
 // (det, t) of bit `bit` of mask word `word`.  Integer shifts and one
 // 32-bit division: 64-bit division would run on the float64 pipe.
@@ -57,18 +73,38 @@ __device__ __forceinline__ void mx_sample(const Segs &segs, int piece, const MxM
     t = s0 + y * piece + (rem / (kBlock / 32)) * kBlock + (rem % (kBlock / 32)) * 32 + bit;
 }
 
-// Calls f(det, t) once for every set bit of the mask, the bits of each 32
-// words dealt out to the 32 lanes of a warp by prefix sum.
-template <class F>
+// Calls f(det, t) once for every set bit of the mask.  A warp reads a
+// window of 32 x kMxWin words (kMxWin independent loads per lane) and deals
+// its set bits out to the 32 lanes by prefix sum, 32 at a time, so that
+// every lane has a sample to work on even where the bits are sparse.  f
+// returns true when it has handled the sample.  With REQUEUE the words are
+// cleared as they are read and the bits whose f returned false set again,
+// so that the next tier's pass over the same mask sees only those: each
+// tier then runs on full warps, instead of a warp paying for a costlier
+// tier whenever one of its lanes needs it.
+template <bool REQUEUE, class F>
 __device__ __forceinline__ void mx_for_each(const Segs &segs, int piece, const MxMask &mm, F &&f) {
     const int lane = threadIdx.x & 31;
-    const long long n_groups = (mm.n_words + 31) / 32;
+    constexpr long long kWinWords = 32LL * kMxWin;
+    const long long n_win = (mm.n_words + kWinWords - 1) / kWinWords;
     const long long warps = (long long)gridDim.x * (blockDim.x / 32);
-    for (long long g = (long long)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
-         g < n_groups; g += warps) {
-        const long long w = g * 32 + lane;
-        const unsigned bits = w < mm.n_words ? mm.words[w] : 0u;
-        const int cnt = __popc(bits);
+    for (long long win = (long long)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+         win < n_win; win += warps) {
+        const long long w0 = win * kWinWords + lane;
+        unsigned bits[kMxWin];
+#pragma unroll
+        for (int i = 0; i < kMxWin; i++) {
+            const long long w = w0 + 32LL * i;
+            bits[i] = w < mm.n_words ? mm.words[w] : 0u;
+        }
+        int cnt = 0;
+#pragma unroll
+        for (int i = 0; i < kMxWin; i++) {
+            cnt += __popc(bits[i]);
+            if (REQUEUE && bits[i]) mm.words[w0 + 32LL * i] = 0u;
+        }
+        if (!__any_sync(kFull, cnt != 0)) continue;
+        if (REQUEUE) __syncwarp();
         int inc = cnt;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
@@ -79,19 +115,34 @@ __device__ __forceinline__ void mx_for_each(const Segs &segs, int piece, const M
         const int excl = inc - cnt;
         for (int base = 0; base < total; base += 32) {
             const int k = base + lane;
-            // Owner: the last lane whose exclusive prefix is <= k.
+            // Owner: the last lane whose exclusive prefix is <= k; then the
+            // owner's word that holds its (k - prefix)-th bit.
             int lo = 0;
 #pragma unroll
             for (int step = 16; step > 0; step >>= 1) {
                 const int e = __shfl_sync(kFull, excl, lo + step);
                 if (e <= k) lo += step;
             }
-            const unsigned ob = __shfl_sync(kFull, bits, lo);
-            const int oe = __shfl_sync(kFull, excl, lo);
+            int r = k - __shfl_sync(kFull, excl, lo), rank = 0, iw = 0;
+            unsigned pick = 0u;
+#pragma unroll
+            for (int i = 0; i < kMxWin; i++) {
+                const unsigned ob = __shfl_sync(kFull, bits[i], lo);
+                const int c = __popc(ob);
+                if (r >= 0 && r < c) {
+                    pick = ob;
+                    rank = r;
+                    iw = i;
+                }
+                r -= c;
+            }
             if (k < total) {
+                const int bit = nth_bit(pick, rank);
+                const long long word = win * kWinWords + 32LL * iw + lo;
                 int det, t;
-                mx_sample(segs, piece, mm, g * 32 + lo, nth_bit(ob, k - oe), det, t);
-                f(det, t);
+                mx_sample(segs, piece, mm, word, bit, det, t);
+                const bool done = f(det, t);
+                if (REQUEUE && !done) atomicOr(mm.words + word, 1u << bit);
             }
         }
     }
@@ -124,13 +175,37 @@ inline bool mx_mask_alloc(MxMask &mm, dim3 grid, int piece, cudaStream_t stream)
 }
 
 // Blocks of kBlock threads for a fallback pass over mask mm: one warp per
-// 32 words, at most 16 waves of 152 SMs (the warps then stride).
+// window of 32 x kMxWin words, at most 8 blocks per SM of 152 (the warps
+// then stride).
 inline unsigned mx_fix_blocks(const MxMask &mm) {
-    const long long groups = (mm.n_words + 31) / 32;
+    const long long windows = (mm.n_words + 32LL * kMxWin - 1) / (32LL * kMxWin);
     const long long warps_per_block = kBlock / 32;
-    long long b = (groups + warps_per_block - 1) / warps_per_block;
-    if (b > 152LL * 16) b = 152LL * 16;
+    long long b = (windows + warps_per_block - 1) / warps_per_block;
+    if (b > 152LL * 8) b = 152LL * 8;
     return (unsigned)(b > 0 ? b : 1);
+}
+
+// Launches the fallback passes k.launch<T> for tiers T = FIRST..2 over
+// mask mm in stream order; the first error stops the sequence.
+template <int FIRST, class K>
+int fix_tiers(const K &k, const MxMask &mm, cudaStream_t stream, const char *what) {
+    const unsigned nb = mx_fix_blocks(mm);
+    int rc = SO3G_OK;
+    if constexpr (FIRST <= 0) {
+        k.template launch<0>(nb, stream);
+        rc = after_launch(what);
+    }
+    if constexpr (FIRST <= 1) {
+        if (rc == SO3G_OK) {
+            k.template launch<1>(nb, stream);
+            rc = after_launch(what);
+        }
+    }
+    if (rc == SO3G_OK) {
+        k.template launch<2>(nb, stream);
+        rc = after_launch(what);
+    }
+    return rc;
 }
 
 }  // namespace
