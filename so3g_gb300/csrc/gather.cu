@@ -545,11 +545,15 @@ struct GatherMxFix {
     }
 };
 
-// The chunked from_map for CAR maps (interp_point.cuh), laid out as
-// k_scatter_ix: the map read from its float32 copy, the signal updated
-// where the sample is certified and on the map, the others marked.
+// The chunked from_map for CAR maps (interp_point.cuh), NC-component map,
+// with four consecutive samples per lane (the layout of k_scatter_ix4), the
+// map read from its float32 copy: one float4 of signal read and written per
+// lane where the row is 16-byte aligned, four independent map reads.
+// Samples it cannot certify keep their value (the fallback passes add
+// theirs) and are marked in the mask.
+template <int NC>
 __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
-    k_from_map_ix(GatherArgs a, MxMask mm, const IxBore *ixb) {
+    k_from_map_ix4(GatherArgs a, MxMask mm, const IxBore *ixb) {
     __shared__ IxParams sp[kBlock / 32][32];
     int det, t0, t1;
     if (!seg_piece(a.segs, a.piece, det, t0, t1)) return;
@@ -558,8 +562,8 @@ __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
     const float q32[4] = {d2f_round(ofs.a), d2f_round(ofs.b), d2f_round(ofs.c),
                           d2f_round(ofs.d)};
     const float T = __ldg(a.resp + 2 * det), Pr = __ldg(a.resp + 2 * det + 1);
-    const int nc = a.g.ncomp;
     float *sig = a.signal + det * a.sig_stride;
+    const bool vec = (reinterpret_cast<unsigned long long>(sig) & 15) == 0;
     unsigned *mwb = mm.words + ((long long)blockIdx.x * gridDim.y + blockIdx.y) * mm.wpp;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int j0 = t0 / kIxLen, j1 = (t1 - 1) / kIxLen + 1;
@@ -567,36 +571,66 @@ __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
         if (g + lane < j1) ix_setup(a, ixb, g + lane, a.segs.n_time, qd, q32, sp[warp][lane]);
         __syncwarp();
         const int nch = min(32, j1 - g);
-        for (int k = 0; k < nch; k++) {
+        const int rounds = (nch + 1) / 2;
+        for (int r = 0; r < rounds; r++) {
+            const int ck = 2 * r + (lane >> 4);
+            const int tq = (g + ck) * kIxLen + (lane & 15) * 4;
+            const bool lane_live = ck < nch;
+            const bool whole = vec && lane_live && tq + 3 < t1;
+            // Loaded before the pointing, so that its latency overlaps it.
+            float sv[4] = {0.f, 0.f, 0.f, 0.f};
+            if (whole) {
+                const float4 v = *reinterpret_cast<const float4 *>(sig + tq);
+                sv[0] = v.x;
+                sv[1] = v.y;
+                sv[2] = v.z;
+                sv[3] = v.w;
+            } else if (lane_live) {
 #pragma unroll
-            for (int h = 0; h < kIxLen / 32; h++) {
-                const int tw = (g + k) * kIxLen + h * 32;
-                const int t = tw + lane;
-                const bool live = t >= t0 && t < t1;
-                // Loaded before the pointing, so that its latency overlaps it.
-                const float s_in = live ? sig[t] : 0.f;
+                for (int i = 0; i < 4; i++)
+                    if (tq + i < t1) sv[i] = sig[tq + i];
+            }
+            const IxParams &pp = sp[warp][min(ck, nch - 1)];
+            unsigned f4 = 0u;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int t = tq + i;
+                const bool live = lane_live && t < t1;
                 int key = 0;
                 bool on = false;
                 float pf[3];
-                const bool ok = ix_eval(sp[warp][k], t, a.g, a.mc, nc, T, Pr, key, on, pf) &&
-                                live;
-                const unsigned fails = __ballot_sync(kFull, live && !ok);
-                if (fails && lane == 0) mwb[(tw - t0) / 32] = fails;
-                if (ok && on) {
+                const bool ok = ix_eval<NC>(pp, t, a.g, a.mc, T, Pr, key, on, pf);
+                if (live && !ok) f4 |= 1u << i;
+                if (live && ok && on) {
                     const float4 m = __ldg(a.map32 + key);
                     // float32 terms (the mixed-precision contract).
-                    float sv = fmaf(m.x, pf[0], s_in);
-                    if (nc > 1) sv = fmaf(m.y, pf[1], sv);
-                    if (nc > 2) sv = fmaf(m.z, pf[2], sv);
-                    sig[t] = sv;
+                    float x = fmaf(m.x, pf[0], sv[i]);
+                    if constexpr (NC > 1) x = fmaf(m.y, pf[1], x);
+                    if constexpr (NC > 2) x = fmaf(m.z, pf[2], x);
+                    sv[i] = x;
                 }
+            }
+            if (__any_sync(kFull, f4 != 0u)) {
+                unsigned x = f4 << (4 * (lane & 7));
+                x |= __shfl_xor_sync(kFull, x, 1);
+                x |= __shfl_xor_sync(kFull, x, 2);
+                x |= __shfl_xor_sync(kFull, x, 4);
+                if ((lane & 7) == 0 && x)
+                    mwb[((g + 2 * r) * kIxLen - t0) / 32 + (lane >> 3)] = x;
+            }
+            if (whole) {
+                *reinterpret_cast<float4 *>(sig + tq) = make_float4(sv[0], sv[1], sv[2], sv[3]);
+            } else if (lane_live) {
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+                    if (tq + i < t1) sig[tq + i] = sv[i];
             }
         }
         __syncwarp();
     }
 }
 
-// Fallback passes of k_from_map_ix, by tier: 0 the float32 tier, 1 the
+// Fallback passes of k_from_map_ix4, by tier: 0 the float32 tier, 1 the
 // double-float pointing (float32 spin factors and terms), 2 the exact
 // float64 pointing, each on the samples the previous tier left.
 template <int TIER>
@@ -654,7 +688,7 @@ int gather_interp(const GatherArgs &a, dim3 grid, cudaStream_t stream) {
     } else {
         const long long npix = (long long)a.g.ny * a.g.nx;
         if (a.segs.seg || a.segs.n_time < 2 || !a.map32 || npix >= (1LL << 31) ||
-            a.piece % kIxLen)
+            a.g.ncomp < 1 || a.g.ncomp > 3 || a.piece % kIxLen)
             return 1;
         IxBore *ixb = ix_bore_models(a.bore, a.segs.n_time, stream);
         if (!ixb) return 1;
@@ -663,7 +697,12 @@ int gather_interp(const GatherArgs &a, dim3 grid, cudaStream_t stream) {
             cudaFreeAsync(ixb, stream);
             return 1;
         }
-        k_from_map_ix<<<grid, kBlock, 0, stream>>>(a, mm, ixb);
+        if (a.g.ncomp == 1)
+            k_from_map_ix4<1><<<grid, kBlock, 0, stream>>>(a, mm, ixb);
+        else if (a.g.ncomp == 2)
+            k_from_map_ix4<2><<<grid, kBlock, 0, stream>>>(a, mm, ixb);
+        else
+            k_from_map_ix4<3><<<grid, kBlock, 0, stream>>>(a, mm, ixb);
         int rc = after_launch("from_map (chunked)");
         if (rc == SO3G_OK) rc = fix_tiers<0>(GatherIxFix{a, mm}, mm, stream, "from_map (chunked fallback)");
         cudaFreeAsync(mm.words, stream);

@@ -61,9 +61,9 @@ struct IxBore {
 struct __align__(16) IxParams {
     float xf, yf, c1r, c1i;     // anchor fractions; z = c1 s + c2 s^2
     float c2r, c2i, z1, z2;     // dZ = s (z1 + s z2)
-    float k1, k2, v0r, v0i;     // dlat = dZ (k1 + k2 dZ); v = v0 + s v1 + s^2 v2
+    float k1, k2, v0r, v0i;     // dlat = dZ (k1 + dZ (k2 + dZ k3)); v = v0 + s v1 + s^2 v2
     float v1r, v1i, v2r, v2i;
-    float bx, by, inv_len;      // bounds (pixels; 2 = chunk not modelled), 1/(tb - ta)
+    float hx, hy, inv_len;      // 1/2 - bounds (pixels; < 0: not modelled), 1/(tb - ta)
     int ta;
     int xb, yb;                 // anchor integer parts
     float k3, pad0;             // dlat's cubic coefficient
@@ -154,7 +154,7 @@ __device__ __forceinline__ void form_v2(const float (&p)[4], const float (&q)[4]
 
 // The model of chunk j for a detector (double-float qd, float32 q32): the
 // anchor from the certified double-float pointing, the coefficients and
-// bounds as described above.  Leaves bx = by = 2 (every sample to the
+// bounds as described above.  Leaves hx = hy = -1 (every sample to the
 // fallback pass) where the model does not apply.
 template <class Args>
 __device__ __forceinline__ void ix_setup(const Args &a, const IxBore *ixb, int j, int n_time,
@@ -169,7 +169,7 @@ __device__ __forceinline__ void ix_setup(const Args &a, const IxBore *ixb, int j
     }
     p.ta = ta;
     p.inv_len = tb > ta ? 1.f / (float)(tb - ta) : 0.f;
-    p.bx = p.by = 2.f;
+    p.hx = p.hy = -1.f;
     const double2 lo = __ldg(reinterpret_cast<const double2 *>(a.bore + 4LL * ta));
     const double2 hi = __ldg(reinterpret_cast<const double2 *>(a.bore + 4LL * ta) + 1);
     dfl qb[4];
@@ -312,17 +312,22 @@ __device__ __forceinline__ void ix_setup(const Args &a, const IxBore *ixb, int j
     p.v1i = v1y;
     p.v2r = v2x;
     p.v2i = v2y;
-    p.bx = bx;
-    p.by = by;
+    p.hx = 0.5f - bx;
+    p.hy = 0.5f - by;
 }
 
 // One sample of a modelled chunk: pixel (key = iy * nx + ix, on = on the
-// map) and spin factors; false when its pixel is not certified.
+// map) and the spin factors of an NC-component map (T; Q, U; or T, Q, U);
+// false when its pixel is not certified.  The fraction r of a pixel
+// coordinate is certified when |r - 1/2| < 1/2 - bound (r - 1/2 and
+// 1/2 - bound are rounded by at most 2^-25, well inside the bound's 1e-7
+// term).
+template <int NC>
 __device__ __forceinline__ bool ix_eval(const IxParams &p, int t, const DGeom &g,
-                                        const MixedConst &mc, int nc, float T, float Pr,
-                                        int &key, bool &on, float *pf) {
+                                        const MixedConst &mc, float T, float Pr, int &key,
+                                        bool &on, float (&pf)[3]) {
     const float4 *w = reinterpret_cast<const float4 *>(&p);
-    const float4 P0 = w[0], P1 = w[1], P2 = w[2], P3 = w[3], P4 = w[4], P5 = w[5];
+    const float4 P0 = w[0], P1 = w[1], P2 = w[2], P4 = w[4], P5 = w[5];
     const float s = (float)(t - __float_as_int(P4.w)) * P4.z;
     const float zr = s * fmaf(s, P1.x, P0.z), zi = s * fmaf(s, P1.y, P0.w);
     // Im(z - z^2/2 + z^3/3) = zi (1 - zr + zr^2 - zi^2/3)
@@ -332,28 +337,28 @@ __device__ __forceinline__ bool ix_eval(const IxParams &p, int t, const DGeom &g
     const float dlat = dz * fmaf(dz, fmaf(dz, P5.z, P2.y), P2.x);
     const float y = fmaf(dlat, mc.inv_cdy, P0.y);
     const float fxl = floorf(x), fyl = floorf(y);
-    const float rx = x - fxl, ry = y - fyl;
-    const bool ok = rx > P4.x && rx < 1.f - P4.x && ry > P4.y && ry < 1.f - P4.y;
+    const bool ok = fabsf((x - fxl) - 0.5f) < P4.x && fabsf((y - fyl) - 0.5f) < P4.y;
     const int ix = __float_as_int(P5.x) + (int)fxl, iy = __float_as_int(P5.y) + (int)fyl;
     on = (unsigned)ix < (unsigned)g.nx && (unsigned)iy < (unsigned)g.ny;
     key = iy * g.nx + ix;
-    if (nc == 1) {
+    if constexpr (NC == 1) {
         pf[0] = T;
         pf[1] = pf[2] = 0.f;
-        return ok;
-    }
-    const float vr = fmaf(s, fmaf(s, P3.z, P3.x), P2.z);
-    const float vi = fmaf(s, fmaf(s, P3.w, P3.y), P2.w);
-    const float k = Pr * rcp_approx(fmaf(vr, vr, vi * vi));
-    const float v1 = fmaf(vr, vr, -vi * vi) * k, v2 = 2.f * vr * vi * k;
-    if (nc == 2) {
-        pf[0] = v1;
-        pf[1] = v2;
-        pf[2] = 0.f;
     } else {
-        pf[0] = T;
-        pf[1] = v1;
-        pf[2] = v2;
+        const float4 P3 = w[3];
+        const float vr = fmaf(s, fmaf(s, P3.z, P3.x), P2.z);
+        const float vi = fmaf(s, fmaf(s, P3.w, P3.y), P2.w);
+        const float k = Pr * rcp_approx(fmaf(vr, vr, vi * vi));
+        const float v1 = fmaf(vr, vr, -vi * vi) * k, v2 = 2.f * vr * vi * k;
+        if constexpr (NC == 2) {
+            pf[0] = v1;
+            pf[1] = v2;
+            pf[2] = 0.f;
+        } else {
+            pf[0] = T;
+            pf[1] = v1;
+            pf[2] = v2;
+        }
     }
     return ok;
 }

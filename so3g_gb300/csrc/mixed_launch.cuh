@@ -160,14 +160,65 @@ __global__ void __launch_bounds__(kBlock) k_scatter_mx_fix(ScatterArgs a, MxMask
     });
 }
 
-// The chunked main pass for CAR maps (interp_point.cuh).  Block (x, y):
-// piece y of detector x; warp w models the groups of 32 chunks g = w, w + 8,
-// ... of the piece (one chunk per lane, parameters in shared memory), then
-// walks their samples 32 at a time (lane = sample).  Samples it cannot
-// certify are marked in the mask as in k_scatter_mx.
-template <bool WEIGHT>
+// Plane offsets (32-bit) and values of one nearest-neighbour sample of an
+// NC-component map: to_map adds sig * pf[c] * det_wt to plane c; to_weight_map
+// adds pf[i] * pf[j] * det_wt to plane i * NC + j (i <= j), as k_scatter
+// (float32 products, left to right).
+template <bool WEIGHT, int NC>
+struct IxValues {
+    static constexpr int NV = WEIGHT ? NC * (NC + 1) / 2 : NC;
+    __device__ static void offsets(int plane, int (&off)[NV]) {
+        if constexpr (!WEIGHT) {
+#pragma unroll
+            for (int c = 0; c < NC; c++) off[c] = c * plane;
+        } else {
+            int k = 0;
+#pragma unroll
+            for (int i = 0; i < NC; i++)
+#pragma unroll
+                for (int j = i; j < NC; j++, k++) off[k] = (i * NC + j) * plane;
+        }
+    }
+    __device__ static void values(float sig, const float (&pf)[3], float det_wt,
+                                  float (&v)[NV]) {
+        if constexpr (!WEIGHT) {
+#pragma unroll
+            for (int c = 0; c < NC; c++) v[c] = sig * pf[c] * det_wt;
+        } else {
+            int k = 0;
+#pragma unroll
+            for (int i = 0; i < NC; i++)
+#pragma unroll
+                for (int j = i; j < NC; j++, k++) v[k] = pf[i] * pf[j] * det_wt;
+        }
+    }
+};
+
+// One run total of k_scatter_ix4 added to the map (key < 0: nothing).
+template <int NV>
+__device__ __forceinline__ void ix_flush_run(int key, const int (&off)[NV], const float (&v)[NV],
+                                             double *map) {
+    if (key >= 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) atomicAdd(map + (key + off[k]), f2d(v[k]));
+    }
+}
+
+// to_map / to_weight_map of the chunked pass with four consecutive samples
+// per lane: round r of a group covers its chunks 2r (lanes 0-15) and 2r + 1
+// (lanes 16-31), one float4 of signal per lane (to_map).  A lane sums the
+// runs of equal pixels among its four samples (right to left, at most four
+// float32 terms: each total within 3u of the exact sum of its terms'
+// magnitudes) and packs them into run slots 0..3; slot j of every lane is
+// flushed with one float64 atomic per component in one pass, taken only
+// when some lane has more than j runs.  Runs are a few samples long, so a
+// round of 128 samples takes about two passes of atomics instead of the
+// four that one sample per lane needs, and a fraction of the L2 atomics.
+// Samples it cannot certify are marked in the mask (bit b of word w = lane
+// 8w + b/4, sample b % 4).
+template <bool WEIGHT, int NC>
 __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
-    k_scatter_ix(ScatterArgs a, MxMask mm, const IxBore *ixb) {
+    k_scatter_ix4(ScatterArgs a, MxMask mm, const IxBore *ixb) {
     __shared__ IxParams sp[kBlock / 32][32];
     int det, t0, t1;
     if (!seg_piece(a.segs, a.piece, det, t0, t1)) return;
@@ -181,51 +232,104 @@ __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
     const float q32[4] = {d2f_round(ofs.a), d2f_round(ofs.b), d2f_round(ofs.c),
                           d2f_round(ofs.d)};
     const float T = __ldg(a.resp + 2 * det), Pr = __ldg(a.resp + 2 * det + 1);
-    const int nc = a.g.ncomp;
-    constexpr int NV = WEIGHT ? 6 : 3;
-    int mult[NV];
-    const unsigned vmask = value_slots<WEIGHT>(nc, mult);
-    const long long plane = (long long)a.g.ny * a.g.nx;
-    const float *sig = a.signal + det * a.sig_stride;
+    using V = IxValues<WEIGHT, NC>;
+    constexpr int NV = V::NV;
+    int off[NV];
+    V::offsets(a.g.ny * a.g.nx, off);
+    const float *sig = WEIGHT ? nullptr : a.signal + det * a.sig_stride;
+    const bool vec = (reinterpret_cast<unsigned long long>(sig) & 15) == 0;
     unsigned *mwb = mm.words + ((long long)blockIdx.x * gridDim.y + blockIdx.y) * mm.wpp;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int j0 = t0 / kIxLen, j1 = (t1 - 1) / kIxLen + 1;
+    // The four samples of this lane from tq, zeros past t1.
+    auto load4 = [&](int tq) {
+        float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (WEIGHT) return r;
+        if (vec && tq + 3 < t1) {
+            r = __ldg(reinterpret_cast<const float4 *>(sig + tq));
+        } else {
+            if (tq < t1) r.x = __ldg(sig + tq);
+            if (tq + 1 < t1) r.y = __ldg(sig + tq + 1);
+            if (tq + 2 < t1) r.z = __ldg(sig + tq + 2);
+            if (tq + 3 < t1) r.w = __ldg(sig + tq + 3);
+        }
+        return r;
+    };
     for (int g = j0 + warp * 32; g < j1; g += (kBlock / 32) * 32) {
         if (g + lane < j1) ix_setup(a, ixb, g + lane, a.segs.n_time, qd, q32, sp[warp][lane]);
         __syncwarp();
         const int nch = min(32, j1 - g);
-        for (int k = 0; k < nch; k++) {
+        const int rounds = (nch + 1) / 2;
+        const int half = lane >> 4;
+        float4 sn = half < nch ? load4((g + half) * kIxLen + (lane & 15) * 4)
+                               : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int r = 0; r < rounds; r++) {
+            const float4 sc = sn;
+            const int ck = 2 * r + half;
+            if (r + 1 < rounds && ck + 2 < nch) sn = load4((g + ck + 2) * kIxLen + (lane & 15) * 4);
+            const int tq = (g + ck) * kIxLen + (lane & 15) * 4;
+            const bool lane_live = ck < nch;
+            const IxParams &pp = sp[warp][min(ck, nch - 1)];
+            const float sg[4] = {sc.x, sc.y, sc.z, sc.w};
+            int key[4];
+            float v[4][NV];
+            unsigned f4 = 0u;
 #pragma unroll
-            for (int h = 0; h < kIxLen / 32; h++) {
-                const int tw = (g + k) * kIxLen + h * 32;
-                const int t = tw + lane;
-                const bool live = t >= t0 && t < t1;
-                const float s_in = (!WEIGHT && live) ? __ldg(sig + t) : 0.f;
-                int key = 0;
+            for (int i = 0; i < 4; i++) {
+                const int t = tq + i;
+                const bool live = lane_live && t < t1;
+                int kk = 0;
                 bool on = false;
                 float pf[3];
-                const bool ok = ix_eval(sp[warp][k], t, a.g, a.mc, nc, T, Pr, key, on, pf) &&
-                                live;
-                const unsigned fails = __ballot_sync(kFull, live && !ok);
-                if (fails && lane == 0) mwb[(tw - t0) / 32] = fails;
-                if (!(ok && on)) key = -1;
-                float v[NV];
-                tap_values<WEIGHT, NV, true>(s_in, pf, 1.f, det_wt, v);
-                if (a.accum == SO3G_ACCUM_WARP_RUNS) {
-                    flush_runs32<NV, kDirectRuns>(key, plane, v, mult, vmask, a.map);
-                } else if (key >= 0) {
-                    double *p = a.map + key;
-#pragma unroll
-                    for (int q = 0; q < NV; q++)
-                        if ((vmask >> q) & 1u) atomicAdd(p + mult[q] * plane, f2d(v[q]));
-                }
+                const bool ok = ix_eval<NC>(pp, t, a.g, a.mc, T, Pr, kk, on, pf);
+                if (live && !ok) f4 |= 1u << i;
+                key[i] = (live && ok && on) ? kk : -1;
+                V::values(sg[i], pf, det_wt, v[i]);
             }
+            if (__any_sync(kFull, f4 != 0u)) {
+                unsigned x = f4 << (4 * (lane & 7));
+                x |= __shfl_xor_sync(kFull, x, 1);
+                x |= __shfl_xor_sync(kFull, x, 2);
+                x |= __shfl_xor_sync(kFull, x, 4);
+                if ((lane & 7) == 0 && x)
+                    mwb[((g + 2 * r) * kIxLen - t0) / 32 + (lane >> 3)] = x;
+            }
+            if (a.accum != SO3G_ACCUM_WARP_RUNS) {
+#pragma unroll
+                for (int i = 0; i < 4; i++) ix_flush_run<NV>(key[i], off, v[i], a.map);
+                continue;
+            }
+            // Run heads and right-to-left run totals (in place: v[i] becomes
+            // the total of the run from i while i is in it).
+            const bool h1 = key[1] != key[0], h2 = key[2] != key[1], h3 = key[3] != key[2];
+#pragma unroll
+            for (int k = 0; k < NV; k++) {
+                if (!h3) v[2][k] += v[3][k];
+                if (!h2) v[1][k] += v[2][k];
+                if (!h1) v[0][k] += v[1][k];
+            }
+            // Slots 1 and 2: the first and second heads among samples 1..3;
+            // slot 3: sample 3 when all three are heads.
+            const int nruns = 1 + h1 + h2 + h3;
+            int ks1 = key[3], ks2 = key[3];
+            float s1[NV], s2[NV];
+#pragma unroll
+            for (int k = 0; k < NV; k++) {
+                s1[k] = h1 ? v[1][k] : (h2 ? v[2][k] : v[3][k]);
+                s2[k] = (h1 && h2) ? v[2][k] : v[3][k];
+            }
+            ks1 = h1 ? key[1] : (h2 ? key[2] : key[3]);
+            ks2 = (h1 && h2) ? key[2] : key[3];
+            ix_flush_run<NV>(key[0], off, v[0], a.map);
+            if (__any_sync(kFull, nruns > 1) && nruns > 1) ix_flush_run<NV>(ks1, off, s1, a.map);
+            if (__any_sync(kFull, nruns > 2) && nruns > 2) ix_flush_run<NV>(ks2, off, s2, a.map);
+            if (__any_sync(kFull, nruns > 3) && nruns > 3) ix_flush_run<NV>(key[3], off, v[3], a.map);
         }
         __syncwarp();
     }
 }
 
-// The fallback passes of k_scatter_ix, by tier: 0 the float32 tier, 1 the
+// The fallback passes of k_scatter_ix4, by tier: 0 the float32 tier, 1 the
 // double-float pointing (float32 spin factors and terms), 2 the exact
 // float64 pointing, each on the samples the previous tier left.
 template <bool WEIGHT, int TIER>
@@ -299,8 +403,10 @@ int scatter_interp(const ScatterArgs &a, dim3 grid, cudaStream_t stream) {
     if constexpr (!(C == SO3G_COORD_CAR && P == PX_FLAT_NT_NN)) {
         return 1;
     } else {
-        const long long npix = (long long)a.g.ny * a.g.nx;
-        if (a.segs.seg || a.segs.n_time < 2 || npix >= (1LL << 31) || a.piece % kIxLen)
+        // Map offsets (key + plane offset) in 32 bits.
+        const long long nc = a.g.ncomp, npix = (long long)a.g.ny * a.g.nx;
+        if (a.segs.seg || a.segs.n_time < 2 || nc < 1 || nc > 3 ||
+            (WEIGHT ? nc * nc : nc) * npix >= (1LL << 31) || a.piece % kIxLen)
             return 1;
         IxBore *ixb = ix_bore_models(a.bore, a.segs.n_time, stream);
         if (!ixb) return 1;
@@ -309,7 +415,12 @@ int scatter_interp(const ScatterArgs &a, dim3 grid, cudaStream_t stream) {
             cudaFreeAsync(ixb, stream);
             return 1;
         }
-        k_scatter_ix<WEIGHT><<<grid, kBlock, 0, stream>>>(a, mm, ixb);
+        if (nc == 1)
+            k_scatter_ix4<WEIGHT, 1><<<grid, kBlock, 0, stream>>>(a, mm, ixb);
+        else if (nc == 2)
+            k_scatter_ix4<WEIGHT, 2><<<grid, kBlock, 0, stream>>>(a, mm, ixb);
+        else
+            k_scatter_ix4<WEIGHT, 3><<<grid, kBlock, 0, stream>>>(a, mm, ixb);
         int rc = after_launch(WEIGHT ? "to_weight_map (chunked)" : "to_map (chunked)");
         if (rc == SO3G_OK)
             rc = fix_tiers<0>(ScatterIxFix<WEIGHT>{a, mm}, mm, stream,

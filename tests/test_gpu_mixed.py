@@ -117,6 +117,47 @@ def test_mixed_maps_within_tolerance(tiled):
         assert np.abs(a - b).max() <= 1e-6 * np.abs(a).max()
 
 
+@pytest.mark.parametrize("ncomp", [1, 2, 3])
+@pytest.mark.parametrize("accum", [_abi.ACCUM_WARP_RUNS, _abi.ACCUM_ATOMIC])
+def test_mixed_to_map_layouts(ncomp, accum):
+    """The chunked CAR to_map / to_weight_map / from_map with signal rows
+    that are not 16-byte aligned (a column slice of a wider array), an odd
+    sample count (a partial last chunk and an odd chunk count per piece),
+    detector weights with zeros, every component count and both
+    accumulation modes, against the exact path."""
+    import torch
+    n_det, n_time = 24, 30_001
+    Q, dets, resp, gamma, sig = synth.workload(n_det, n_time, seed=59, radius_deg=1.0)
+    p, eng = _engine((600, 600), ARCMIN, False, ncomp=ncomp)
+    q = synth.native(p, Q)
+    qd, dd, rd = (torch.from_numpy(x).cuda() for x in (q, dets, resp))
+    wide = torch.zeros((n_det, n_time + 1), dtype=torch.float32, device="cuda")
+    wide[:, 1:] = torch.from_numpy(sig).cuda()
+    sv = wide[:, 1:]
+    assert sv.data_ptr() % 16 != 0 and sv.stride(0) == n_time + 1
+    w = np.linspace(0., 2., n_det).astype(np.float32)
+    w[7] = 0.
+    wd = torch.from_numpy(w).cuda()
+    shape = eng._pix_shape()
+    out = {}
+    for mode in MODES:
+        eng.pointing = mode
+        m = eng.to_map(torch.zeros((ncomp,) + shape, dtype=torch.float64, device="cuda"), qd, dd,
+                       rd, sv, wd, None, accum=accum)
+        ww = eng.to_weight_map(torch.zeros((ncomp, ncomp) + shape, dtype=torch.float64,
+                                           device="cuda"), qd, dd, rd, wd, None, accum=accum)
+        base = torch.full((n_det, n_time + 1), 0.5, dtype=torch.float32, device="cuda")
+        back = eng.from_map(out[_abi.POINTING_EXACT][0] if out else m, qd, dd, rd, base[:, 1:])
+        out[mode] = [m, ww, back]
+    for a, b in zip(out[_abi.POINTING_EXACT], out[_abi.POINTING_MIXED]):
+        a, b = a.double().cpu().numpy(), b.double().cpu().numpy()
+        assert np.abs(a - b).max() <= 1e-6 * np.abs(a).max()
+    # The strided signal was read, not copied: the zero-weight detector adds
+    # nothing, the others something.
+    m = out[_abi.POINTING_MIXED][0]
+    assert float(m.abs().sum()) > 0
+
+
 def _probe_hp(eng, q, dets, resp, tiled, pf_bound=PF_BOUND_GUARD):
     import torch
     from test_gpu_certified import _hp_probe_maps
