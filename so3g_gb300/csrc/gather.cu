@@ -599,7 +599,7 @@ __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
                 int key = 0;
                 bool on = false;
                 float pf[3];
-                const bool ok = ix_eval<NC>(pp, t, a.g, a.mc, T, Pr, key, on, pf);
+                const bool ok = ix_eval<NC>(pp, ix_s(pp, tq, i), a.g, T, Pr, key, on, pf);
                 if (live && !ok) f4 |= 1u << i;
                 if (live && ok && on) {
                     const float4 m = __ldg(a.map32 + key);

@@ -14,18 +14,21 @@
 //   Z = a^2 - b^2 - c^2 + d^2,            lat = asin(Z)
 //   v = Nc + iNs = (ac - bd) + i(cd + ab), the spin factors P v^2 / |v|^2
 // so along the model each is a polynomial in s, of degree 4 with its s^3
-// and s^4 coefficients negligible (|A2| ~ 1e-6): per sample,
+// and s^4 coefficients negligible (|A2| ~ 1e-6):
 //   lon = lon(ta) + arg(1 + z),  z = c1 s + c2 s^2 (c_k = W_k / W_0)
 //         ~ lon(ta) + Im(z - z^2/2 + z^3/3)              (|z| < 0.05)
 //   lat = lat(ta) + k1 dZ + k2 dZ^2 + k3 dZ^3,  dZ = s Z1 + s^2 Z2
-//         (asin's Taylor series)
-// in about 40 float32 operations, with no boresight load and no table.
+//         (asin's Taylor series),
+// both expanded in s and cut after s^3: per sample a cubic in s for each
+// pixel coordinate and a quadratic for each spin component, about 25
+// float32 operations, with no boresight load and no table.
 // The anchor lon(ta), lat(ta) are the reference's values at ta from the
 // certified double-float pointing (fastpoint.cuh), as pixel coordinates
 // x(ta), y(ta) split into an integer and a fraction.
 //
 // Bound (ix_setup): the remainders of the two series (|z|^4 / (4(1-|z|))
-// and the asin term |dZ|^4 max|asin''''| / 24), the dropped s^3, s^4 terms
+// and the asin term |dZ|^4 max|asin''''| / 24), the terms cut from their
+// expansions in s, the dropped s^3, s^4 terms
 // and the model error E through the forms' norms (|B_w(p, q)| <= |p||q|/
 // sqrt(2), |B_Z(p, q)| <= |p||q|), the float32 evaluation of the
 // coefficients and of the per-sample polynomials, the reference's table
@@ -56,17 +59,15 @@ struct IxBore {
     float pad[3];
 };
 
-// Per (detector, chunk): the model's coefficients and bounds, read by every
-// lane of a warp (six 16-byte words).
+// Per (detector, chunk): the model's coefficients and bounds, read by the
+// lanes of a chunk (five 16-byte words).
 struct __align__(16) IxParams {
-    float xf, yf, c1r, c1i;     // anchor fractions; z = c1 s + c2 s^2
-    float c2r, c2i, z1, z2;     // dZ = s (z1 + s z2)
-    float k1, k2, v0r, v0i;     // dlat = dZ (k1 + dZ (k2 + dZ k3)); v = v0 + s v1 + s^2 v2
-    float v1r, v1i, v2r, v2i;
-    float hx, hy, inv_len;      // 1/2 - bounds (pixels; < 0: not modelled), 1/(tb - ta)
-    int ta;
-    int xb, yb;                 // anchor integer parts
-    float k3, pad0;             // dlat's cubic coefficient
+    float xf, yf, b1, b2;       // x = xb + xf + s (b1 + s (b2 + s b3)) (pixels)
+    float b3, e1, e2, e3;       // y = yb + yf + s (e1 + s (e2 + s e3))
+    float v0r, v0i, v1r, v1i;   // v = v0 + s v1 + s^2 v2
+    float v2r, v2i, hx, hy;     // 1/2 - bounds (pixels; < 0: not modelled)
+    float inv_len;              // 1 / (tb - ta)
+    int ta, xb, yb;             // chunk start; the anchor's integer parts
 };
 
 // The chunks' boresight models (one thread per chunk), in float64.
@@ -165,7 +166,7 @@ __device__ __forceinline__ void ix_setup(const Args &a, const IxBore *ixb, int j
     {
         float4 *w = reinterpret_cast<float4 *>(&p);
 #pragma unroll
-        for (int k = 0; k < 6; k++) w[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int k = 0; k < (int)(sizeof(IxParams) / 16); k++) w[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     p.ta = ta;
     p.inv_len = tb > ta ? 1.f / (float)(tb - ta) : 0.f;
@@ -228,23 +229,38 @@ __device__ __forceinline__ void ix_setup(const Args &a, const IxBore *ixb, int j
     const float c2r = (w2x * w0x + w2y * w0y) * ir, c2i = (w2y * w0x - w2x * w0y) * ir;
     const float s2 = 1.41421356f;
     const float eta = (s2 * n1 * n2 + n2 * n2 / s2 + s2 * Em * E + E * E / s2) / w0a;
-    const float zmax = sqrtf(c1r * c1r + c1i * c1i) + sqrtf(c2r * c2r + c2i * c2i) + eta +
-                       ecoef / w0a;
+    const float c1a = sqrtf(c1r * c1r + c1i * c1i), c2a = sqrtf(c2r * c2r + c2i * c2i);
+    const float zmax = c1a + c2a + eta + ecoef / w0a;
     if (!(zmax < 0.05f)) return;
     const float dlmax = zmax * (1.f + zmax);
     // atan2 seam: lon stays inside (-pi, pi) over the chunk.
     if (!(fabsf(X.hi) + dlmax < 3.1405f)) return;
-    // Series remainder, the dropped terms (eta) and the coefficients'
-    // errors through the series' derivative (<= 1 + 2|z|): W1, W2's
-    // absolute errors, W0's relative error, the division's roundings (6u
-    // |c|) and the per-sample evaluation (6u |z|); and the ATAN2 table's
-    // interpolation error at both ends (h^2/8 max|atan''| = 3.0e-10).
+    // Per sample the series Im(z - z^2/2 + z^3/3), z = c1 s + c2 s^2, is
+    // evaluated as its expansion in s cut after s^3 (pixels: x = xf +
+    // s (b1 + s (b2 + s b3))):
+    //   b1 = Im c1,  b2 = Im c2 - Im(c1^2)/2,  b3 = Im(c1^3)/3 - Im(c1 c2);
+    // the cut s^4..s^6 terms are within |c2| (|c1|^2 + |c1||c2| + |c2|^2/3
+    // + |c2|/2).
+    const float icxs = a.mc.inv_cdx, icys = a.mc.inv_cdy;
+    const float b1 = c1i * icxs;
+    const float b2 = (c2i - c1r * c1i) * icxs;
+    const float b3 = (c1i * (c1r * c1r - c1i * c1i * (1.f / 3.f)) - (c1r * c2i + c1i * c2r)) * icxs;
+    const float cut_lon = c2a * (c1a * (c1a + c2a) + c2a * (c2a * (1.f / 3.f) + 0.5f));
+    // Series remainder, the cut terms, the dropped terms (eta) and the
+    // coefficients' errors through the series' derivative (<= 1 + 2|z|):
+    // W1, W2's absolute errors, W0's relative error and the division's
+    // roundings (6u |c|); and the ATAN2 table's interpolation error at both
+    // ends (h^2/8 max|atan''| = 3.0e-10).
     const float z2m = zmax * zmax;
-    const float lon_err = z2m * z2m / (4.f * (1.f - zmax)) + eta * (1.f + 2.f * zmax) +
-                          (ecoef / w0a + (rel0 / w0a + 12.f * u) * zmax) * (1.f + 2.f * zmax) +
+    const float lon_err = z2m * z2m / (4.f * (1.f - zmax)) + cut_lon + eta * (1.f + 2.f * zmax) +
+                          (ecoef / w0a + (rel0 / w0a + 6.f * u) * zmax) * (1.f + 2.f * zmax) +
                           2.f * 3.1e-10f;
-    const float icx = fabsf(a.mc.inv_cdx), icy = fabsf(a.mc.inv_cdy);
-    const float bx = 1.5f * (lon_err * icx + 1e-7f + u * (2.f * dlmax * icx + 2.f));
+    const float icx = fabsf(icxs), icy = fabsf(icys);
+    // In pixels: lon_err, the roundings of b1..b3 (<= 5u each, |b1| + |b2|
+    // + |b3| <= (zmax + zmax^2 + zmax^3) / cdelt), of the float32 1/cdelt
+    // and of the per-sample Horner steps (4u of dlmax / cdelt, u of x).
+    const float bx = 1.5f * (lon_err * icx + 1e-7f + 8.f * u * zmax * (1.f + zmax) * icx +
+                             u * (4.f * dlmax * icx + 2.f));
 
     // Latitude: Z(s) = Z0 + Z1 s + Z2 s^2 (+ Z3 s^3 + Z4 s^4).
     const float Z0 = form_z(A0);
@@ -271,15 +287,26 @@ __device__ __forceinline__ void ix_setup(const Args &a, const IxBore *ixb, int j
     // h = 1 / (kLutN - 1).
     const float h2_8 = 1.f / (8.f * 16383.f * 16383.f);
     const float dz2 = dzmax * dzmax;
-    // Series remainder; dZ's errors through the series' derivative; Z0's
-    // error through the coefficients (d k_n / dZ0 = (n + 1) k_(n+1)); the
-    // roundings of the coefficients and of the per-sample evaluation
-    // (32u |dlat|); the ASIN table at both ends and the anchor.
-    const float lat_err = dz2 * dz2 * m4 / 24.f +
+    // Per sample k1 dZ + k2 dZ^2 + k3 dZ^3, dZ = Z1 s + Z2 s^2, is evaluated
+    // as its expansion in s cut after s^3 (pixels: y = yf + s (e1 + s (e2
+    // + s e3))):  e1 = k1 Z1,  e2 = k1 Z2 + k2 Z1^2,  e3 = 2 k2 Z1 Z2 +
+    // k3 Z1^3;  the cut terms are within k2 Z2^2 + k3 |Z2| (3 Z1^2 + 3 |Z1
+    // Z2| + Z2^2).
+    const float Z1a = fabsf(Z1), Z2a = fabsf(Z2);
+    const float e1 = k1 * Z1 * icys;
+    const float e2 = (k1 * Z2 + k2 * Z1 * Z1) * icys;
+    const float e3 = (2.f * k2 * Z1 * Z2 + k3 * Z1 * Z1 * Z1) * icys;
+    const float cut_lat = k2m * Z2a * Z2a + k3m * Z2a * (3.f * Z1a * (Z1a + Z2a) + Z2a * Z2a);
+    // Series remainder; the cut terms; dZ's errors through the series'
+    // derivative; Z0's error through the coefficients (d k_n / dZ0 = (n + 1)
+    // k_(n+1)); the roundings of k1..k3 and e1..e3 (32u |dlat|); the ASIN
+    // table at both ends and the anchor.
+    const float lat_err = dz2 * dz2 * m4 / 24.f + cut_lat +
                           (etaZ + ecoef) * (k1m + 2.f * k2m * dzm + 3.f * k3m * dzm * dzm) +
                           dZ0 * dzm * (2.f * k2m + dzm * (3.f * k3m + dzm * m4 / 6.f)) +
                           32.f * u * dlatmax + 2.f * (h2_8 * Zm * r3 + 1e-15f);
-    const float by = 1.5f * (lat_err * icy + 1e-7f + u * (2.f * dlatmax * icy + 2.f));
+    // In pixels, with the float32 1/cdelt and the Horner steps.
+    const float by = 1.5f * (lat_err * icy + 1e-7f + u * (4.f * dlatmax * icy + 2.f));
 
     // Spin: v(s) = V0 + V1 s + V2 s^2; the dropped terms and the model
     // error must stay below 1e-7 of |v| for the float32 contract.
@@ -297,15 +324,12 @@ __device__ __forceinline__ void ix_setup(const Args &a, const IxBore *ixb, int j
     p.yf = fy.hi + fy.lo;
     p.xb = xb;
     p.yb = yb;
-    p.c1r = c1r;
-    p.c1i = c1i;
-    p.c2r = c2r;
-    p.c2i = c2i;
-    p.z1 = Z1;
-    p.z2 = Z2;
-    p.k1 = k1;
-    p.k2 = k2;
-    p.k3 = k3;
+    p.b1 = b1;
+    p.b2 = b2;
+    p.b3 = b3;
+    p.e1 = e1;
+    p.e2 = e2;
+    p.e3 = e3;
     p.v0r = v0x;
     p.v0i = v0y;
     p.v1r = v1x;
@@ -316,38 +340,32 @@ __device__ __forceinline__ void ix_setup(const Args &a, const IxBore *ixb, int j
     p.hy = 0.5f - by;
 }
 
-// One sample of a modelled chunk: pixel (key = iy * nx + ix, on = on the
-// map) and the spin factors of an NC-component map (T; Q, U; or T, Q, U);
-// false when its pixel is not certified.  The fraction r of a pixel
-// coordinate is certified when |r - 1/2| < 1/2 - bound (r - 1/2 and
-// 1/2 - bound are rounded by at most 2^-25, well inside the bound's 1e-7
-// term).
+// One sample of a modelled chunk at s = (t - ta) / (tb - ta) (computed by
+// the caller as (float)(t - ta) * inv_len: within 2u of s): pixel (key =
+// iy * nx + ix, on = on the map) and the spin factors of an NC-component
+// map (T; Q, U; or T, Q, U); false when its pixel is not certified.  The
+// fraction r of a pixel coordinate is certified when |r - 1/2| < 1/2 -
+// bound (r - 1/2 and 1/2 - bound are rounded by at most 2^-25, well inside
+// the bound's 1e-7 term).
 template <int NC>
-__device__ __forceinline__ bool ix_eval(const IxParams &p, int t, const DGeom &g,
-                                        const MixedConst &mc, float T, float Pr, int &key,
-                                        bool &on, float (&pf)[3]) {
+__device__ __forceinline__ bool ix_eval(const IxParams &p, float s, const DGeom &g, float T,
+                                        float Pr, int &key, bool &on, float (&pf)[3]) {
     const float4 *w = reinterpret_cast<const float4 *>(&p);
-    const float4 P0 = w[0], P1 = w[1], P2 = w[2], P4 = w[4], P5 = w[5];
-    const float s = (float)(t - __float_as_int(P4.w)) * P4.z;
-    const float zr = s * fmaf(s, P1.x, P0.z), zi = s * fmaf(s, P1.y, P0.w);
-    // Im(z - z^2/2 + z^3/3) = zi (1 - zr + zr^2 - zi^2/3)
-    const float dl = zi * fmaf(-0.33333334f * zi, zi, fmaf(zr, zr - 1.f, 1.f));
-    const float x = fmaf(dl, mc.inv_cdx, P0.x);
-    const float dz = s * fmaf(s, P1.w, P1.z);
-    const float dlat = dz * fmaf(dz, fmaf(dz, P5.z, P2.y), P2.x);
-    const float y = fmaf(dlat, mc.inv_cdy, P0.y);
+    const float4 P0 = w[0], P1 = w[1], P3 = w[3], P4 = w[4];
+    const float x = fmaf(s, fmaf(s, fmaf(s, P1.x, P0.w), P0.z), P0.x);
+    const float y = fmaf(s, fmaf(s, fmaf(s, P1.w, P1.z), P1.y), P0.y);
     const float fxl = floorf(x), fyl = floorf(y);
-    const bool ok = fabsf((x - fxl) - 0.5f) < P4.x && fabsf((y - fyl) - 0.5f) < P4.y;
-    const int ix = __float_as_int(P5.x) + (int)fxl, iy = __float_as_int(P5.y) + (int)fyl;
+    const bool ok = fabsf((x - fxl) - 0.5f) < P3.z && fabsf((y - fyl) - 0.5f) < P3.w;
+    const int ix = __float_as_int(P4.z) + (int)fxl, iy = __float_as_int(P4.w) + (int)fyl;
     on = (unsigned)ix < (unsigned)g.nx && (unsigned)iy < (unsigned)g.ny;
     key = iy * g.nx + ix;
     if constexpr (NC == 1) {
         pf[0] = T;
         pf[1] = pf[2] = 0.f;
     } else {
-        const float4 P3 = w[3];
-        const float vr = fmaf(s, fmaf(s, P3.z, P3.x), P2.z);
-        const float vi = fmaf(s, fmaf(s, P3.w, P3.y), P2.w);
+        const float4 P2 = w[2];
+        const float vr = fmaf(s, fmaf(s, P3.x, P2.z), P2.x);
+        const float vi = fmaf(s, fmaf(s, P3.y, P2.w), P2.y);
         const float k = Pr * rcp_approx(fmaf(vr, vr, vi * vi));
         const float v1 = fmaf(vr, vr, -vi * vi) * k, v2 = 2.f * vr * vi * k;
         if constexpr (NC == 2) {
@@ -361,6 +379,13 @@ __device__ __forceinline__ bool ix_eval(const IxParams &p, int t, const DGeom &g
         }
     }
     return ok;
+}
+
+// s of sample tq + i of a chunk: (float)(tq + i - ta) * inv_len, the
+// difference formed exactly (|tq - ta| < 2^24).
+__device__ __forceinline__ float ix_s(const IxParams &p, int tq, int i) {
+    const float4 P4 = reinterpret_cast<const float4 *>(&p)[4];
+    return ((float)(tq - __float_as_int(P4.y)) + (float)i) * P4.x;
 }
 
 // The boresight models of a call's chunks, in stream-ordered memory; NULL

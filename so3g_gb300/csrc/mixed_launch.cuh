@@ -281,7 +281,7 @@ __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
                 int kk = 0;
                 bool on = false;
                 float pf[3];
-                const bool ok = ix_eval<NC>(pp, t, a.g, a.mc, T, Pr, kk, on, pf);
+                const bool ok = ix_eval<NC>(pp, ix_s(pp, tq, i), a.g, T, Pr, kk, on, pf);
                 if (live && !ok) f4 |= 1u << i;
                 key[i] = (live && ok && on) ? kk : -1;
                 V::values(sg[i], pf, det_wt, v[i]);
