@@ -609,19 +609,8 @@ __device__ __forceinline__ bool fast_pointing(const DGeom &g, const FastTables &
     return fast_spin<SPIN_CERT>(nc, T, Pr, Nc, Ns, D, pf);
 }
 
-// sig + m * pf rounded to float32 as the reference's `*sig += map * pf`
-// (float64 product and sum, then float32) when that rounding is certain.
-// Returns false when it is not (the caller then takes the exact path).
-__device__ __forceinline__ bool fast_accum(float &sig, double m, float pf) {
-    const int mh = __double2hiint(m);
-    if ((((unsigned)mh & 0x7fffffffu) | (unsigned)__double2loint(m)) == 0u || pf == 0.f) {
-        // The term is an exact zero with the product's sign; float addition
-        // of zeros follows the same sign rules as the reference's float64.
-        sig = sig + __int_as_float((mh ^ __float_as_int(pf)) & 0x80000000);
-        return true;
-    }
-    dfl md;
-    if (!df_split(m, md)) return false;
+// The rounding step of fast_accum from m's double-float split md.
+__device__ __forceinline__ bool fast_accum_df(float &sig, dfl md, float pf) {
     const float p = md.hi * pf;
     float pe = fmaf(md.hi, pf, -p);
     pe = fmaf(md.lo, pf, pe);
@@ -634,6 +623,34 @@ __device__ __forceinline__ bool fast_accum(float &sig, double m, float pf) {
     if (!(fabsf(s.hi) > 1e-30f && fabsf(s.lo) + e < half_gap(s.hi))) return false;
     sig = s.hi;
     return true;
+}
+
+// sig + m * pf rounded to float32 as the reference's `*sig += map * pf`
+// (float64 product and sum, then float32) when that rounding is certain.
+// Returns false when it is not (the caller then takes the exact path).
+__device__ __forceinline__ bool fast_accum(float &sig, double m, float pf) {
+    const int mh = __double2hiint(m);
+    if ((((unsigned)mh & 0x7fffffffu) | (unsigned)__double2loint(m)) == 0u ||
+        (pf == 0.f && (mh & 0x7ff00000) != 0x7ff00000)) {
+        // The term is an exact zero with the product's sign (0 times a
+        // finite value); float addition of zeros follows the same sign rules
+        // as the reference's float64.
+        sig = sig + __int_as_float((mh ^ __float_as_int(pf)) & 0x80000000);
+        return true;
+    }
+    dfl md;
+    if (!df_split(m, md)) return false;
+    return fast_accum_df(sig, md, pf);
+}
+
+// The same with m given by its split (h, l) (k_pc_map_split): h = +-0 for
+// m = +-0, NaN where m is not finite or outside df_split's range.
+__device__ __forceinline__ bool fast_accum_split(float &sig, float h, float l, float pf) {
+    if (h == 0.f || (pf == 0.f && h == h)) {
+        sig = sig + __int_as_float((__float_as_int(h) ^ __float_as_int(pf)) & 0x80000000);
+        return true;
+    }
+    return fast_accum_df(sig, dfl{h, l}, pf);
 }
 
 // The same for a bilinear tap: sig + m * pf * w as the reference's

@@ -5,6 +5,8 @@
 // the vectorised kernels (k_pc_scatter4, k_pc_from_map4); everything else
 // the per-sample ones.
 
+#include <algorithm>
+
 #include "host.h"
 
 namespace so3g {
@@ -360,10 +362,58 @@ __global__ void __launch_bounds__(kBlock) k_pc_scatter4(PcArgs a) {
     }
 }
 
-// Compiled for 8 resident blocks per SM (32 registers, full occupancy):
-// measured 6 % faster than the unbounded 56-register form.
+// float4 words per pixel of the split map of an NC-component map.
 template <int NC>
-__global__ void __launch_bounds__(kBlock, 8) k_pc_from_map4(PcArgs a) {
+struct PcSplit {
+    static constexpr int W = (NC + 1) / 2;
+};
+
+// The map split for k_pc_from_map4: per pixel, component c's float64
+// value m as df_split's double-float (h, l) at words 2c, 2c + 1 (h = +-0 for
+// m = +-0; NaN where m is not finite or outside df_split's range, which
+// sends the sample to the float64 arithmetic), pixel-major: one sample
+// reads its pixel's NC components from one or two float4 instead of NC
+// float64 planes, and needs no split of its own.
+template <int NC>
+__global__ void k_pc_map_split(const double *map, long long plane, float4 *split) {
+    constexpr int W = PcSplit<NC>::W;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < plane;
+         p += (long long)gridDim.x * blockDim.x) {
+        float hl[4 * W];
+#pragma unroll
+        for (int k = 0; k < 4 * W; k++) hl[k] = 0.f;
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            const double m = __ldg(map + c * plane + p);
+            const unsigned mh = (unsigned)__double2hiint(m);
+            float h = __int_as_float(0x7fc00000), l = 0.f;
+            if (((mh & 0x7fffffffu) | (unsigned)__double2loint(m)) == 0u) {
+                h = __uint_as_float(mh & 0x80000000u);
+            } else {
+                dfl d;
+                if (df_split(m, d)) {
+                    h = d.hi;
+                    l = d.lo;
+                }
+            }
+            hl[2 * c] = h;
+            hl[2 * c + 1] = l;
+        }
+#pragma unroll
+        for (int w = 0; w < W; w++)
+            split[p * W + w] = make_float4(hl[4 * w], hl[4 * w + 1], hl[4 * w + 2], hl[4 * w + 3]);
+    }
+}
+
+// With SPLIT (the form the launcher takes) the map values come from
+// k_pc_map_split's copy, the float64 map only for a sample whose rounding is
+// not certain: 4.60 ms against 6.15 ms for the kernel that splits each
+// value itself (1000 det x 1M samples, 3x2000x2000 map), compiled for 6
+// resident blocks (40 registers; 8 blocks spill: 5.23 ms, 5 blocks: 4.70
+// ms).  Without SPLIT (no memory for the copy): 8 blocks, 32 registers.
+template <int NC, bool SPLIT>
+__global__ void __launch_bounds__(kBlock, SPLIT ? 6 : 8)
+    k_pc_from_map4(PcArgs a, const float4 *split) {
     // ProjEng_Precomp::from_map, src/Projection.cxx:2066-2082
     int det, t0, t1;
     if (!seg_piece(a.segs, a.piece, det, t0, t1)) return;
@@ -386,18 +436,39 @@ __global__ void __launch_bounds__(kBlock, 8) k_pc_from_map4(PcArgs a) {
             // float32: certified double-float roundings, fast_accum; the
             // float64 arithmetic itself where one is uncertain), then adds
             // sig to the signal.
-            double mv[NC];
             float s1 = 0.f;
             bool ok = true;
+            if (SPLIT) {
+                constexpr int W = PcSplit<NC>::W;
+                float hl[4 * W];
 #pragma unroll
-            for (int c = 0; c < NC; c++) {
-                mv[c] = __ldg(a.map + off + c * plane);
-                ok = ok && fast_accum(s1, mv[c], pf[c]);
-            }
-            if (!ok) {
-                s1 = 0.f;
+                for (int w = 0; w < W; w++) {
+                    const float4 q = __ldg(split + off * W + w);
+                    hl[4 * w] = q.x;
+                    hl[4 * w + 1] = q.y;
+                    hl[4 * w + 2] = q.z;
+                    hl[4 * w + 3] = q.w;
+                }
 #pragma unroll
-                for (int c = 0; c < NC; c++) s1 += pf[c] * mv[c];
+                for (int c = 0; c < NC; c++)
+                    ok = ok && fast_accum_split(s1, hl[2 * c], hl[2 * c + 1], pf[c]);
+                if (!ok) {
+                    s1 = 0.f;
+#pragma unroll
+                    for (int c = 0; c < NC; c++) s1 += pf[c] * __ldg(a.map + off + c * plane);
+                }
+            } else {
+                double mv[NC];
+#pragma unroll
+                for (int c = 0; c < NC; c++) {
+                    mv[c] = __ldg(a.map + off + c * plane);
+                    ok = ok && fast_accum(s1, mv[c], pf[c]);
+                }
+                if (!ok) {
+                    s1 = 0.f;
+#pragma unroll
+                    for (int c = 0; c < NC; c++) s1 += pf[c] * mv[c];
+                }
             }
             sig[j] += s1;
         }
@@ -421,11 +492,32 @@ void pc_scatter4_launch(const PcArgs &a, dim3 grid, cudaStream_t st) {
     }
 }
 
+template <int NC>
+void pc_from_map4_nc(const PcArgs &a, dim3 grid, cudaStream_t st) {
+    // The split map (W float4 per pixel) in stream-ordered memory; without
+    // it, the kernel splits each map value itself.
+    const long long plane = (long long)a.ny * a.nx;
+    float4 *split = nullptr;
+    if (cudaMallocAsync(reinterpret_cast<void **>(&split),
+                        sizeof(float4) * PcSplit<NC>::W * (size_t)plane, st) != cudaSuccess) {
+        cudaGetLastError();
+        split = nullptr;
+    }
+    if (split) {
+        const long long blocks = std::min<long long>((plane + kBlock - 1) / kBlock, 152LL * 16);
+        k_pc_map_split<NC><<<(unsigned)blocks, kBlock, 0, st>>>(a.map, plane, split);
+        k_pc_from_map4<NC, true><<<grid, kBlock, 0, st>>>(a, split);
+        cudaFreeAsync(split, st);
+    } else {
+        k_pc_from_map4<NC, false><<<grid, kBlock, 0, st>>>(a, nullptr);
+    }
+}
+
 void pc_from_map4_launch(const PcArgs &a, dim3 grid, cudaStream_t st) {
     switch (a.nc) {
-    case 1: k_pc_from_map4<1><<<grid, kBlock, 0, st>>>(a); break;
-    case 2: k_pc_from_map4<2><<<grid, kBlock, 0, st>>>(a); break;
-    default: k_pc_from_map4<3><<<grid, kBlock, 0, st>>>(a); break;
+    case 1: pc_from_map4_nc<1>(a, grid, st); break;
+    case 2: pc_from_map4_nc<2>(a, grid, st); break;
+    default: pc_from_map4_nc<3>(a, grid, st); break;
     }
 }
 

@@ -95,11 +95,12 @@ def test_precomp_pixel_out_of_range(orc, gpulib):
         pe.to_map(np.zeros((3, 4, 5)), pix, proj, np.ones((1, 10), np.float32), None, None)
 
 
-@pytest.mark.parametrize("n_time", [3000, 3004, 3001])
+@pytest.mark.parametrize("n_time", [3000, 3004, 3001, 9000])
 @pytest.mark.parametrize("ncomp", [1, 2, 3])
 def test_precomp_vector_and_scalar_paths(orc, gpulib, n_time, ncomp):
     """n_time a multiple of 4 (16-byte aligned rows): the vectorised
-    kernels; otherwise the per-sample ones.  Both against the oracle: maps
+    kernels, over one piece or several (9000 samples: pieces of 4096);
+    otherwise the per-sample ones.  Both against the oracle: maps
     to float64 summation order, from_map into a non-zero signal bit for bit,
     with samples off the map (negative pixel) and detector weights."""
     import torch
