@@ -282,14 +282,14 @@ class ClockSampler:
 # DRAM bytes per sample (dram__bytes_read.sum + dram__bytes_write.sum / samples)
 # of one ncu capture of the to_map and from_map kernels, CAR TQU 3x2000x2000,
 # 200 det x 1M samples, per pointing mode (profiles/to_map_from_map_*_car_
-# tqu_200det_1M.md).  The traffic is the signal (4 B read, from_map also 4 B
-# written), the boresight per detector and (mixed to_map) spilled registers,
-# so it scales with the samples.
+# tqu_200det_1M.md; mixed: the chunked main kernels k_scatter_ix4 and
+# k_from_map_ix4).  The traffic is the signal (4 B read, from_map also 4 B
+# written) and the boresight per detector, so it scales with the samples.
 MEASURED_TRAFFIC_PER_SAMPLE = {
     "certified": {"to_map": (834.33e6 + 3.78e6) / 2e8,
                   "from_map": (835.40e6 + 747.14e6) / 2e8},
-    "mixed": {"to_map": (883.75e6 + 110.41e6) / 2e8,
-              "from_map": (859.73e6 + 844.40e6) / 2e8},
+    "mixed": {"to_map": (809.487e6 + 9.860e6) / 2e8,
+              "from_map": (809.183e6 + 752.803e6) / 2e8},
 }
 # Float64-pipe lane operations per sample of the float64 path's to_map
 # (ncu sm__inst_executed_pipe_fp64.sum x 32 / samples, 200 detectors x 1M)
