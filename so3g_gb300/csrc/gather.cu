@@ -551,7 +551,7 @@ struct GatherMxFix {
 // lane where the row is 16-byte aligned, four independent map reads.
 // Samples it cannot certify keep their value (the fallback passes add
 // theirs) and are marked in the mask.
-template <int NC>
+template <int P, int NC>
 __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
     k_from_map_ix4(GatherArgs a, MxMask mm, const IxBore *ixb) {
     __shared__ IxParams sp[kBlock / 32][32];
@@ -568,7 +568,8 @@ __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int j0 = t0 / kIxLen, j1 = (t1 - 1) / kIxLen + 1;
     for (int g = j0 + warp * 32; g < j1; g += (kBlock / 32) * 32) {
-        if (g + lane < j1) ix_setup(a, ixb, g + lane, a.segs.n_time, qd, q32, sp[warp][lane]);
+        if (g + lane < j1)
+            ix_setup<P == PX_HP_NT>(a, ixb, g + lane, a.segs.n_time, qd, q32, sp[warp][lane]);
         __syncwarp();
         const int nch = min(32, j1 - g);
         const int rounds = (nch + 1) / 2;
@@ -599,7 +600,7 @@ __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
                 int key = 0;
                 bool on = false;
                 float pf[3];
-                const bool ok = ix_eval<NC>(pp, ix_s(pp, tq, i), a.g, T, Pr, key, on, pf);
+                const bool ok = ix_sample<P, NC>(pp, ix_s(pp, tq, i), a.g, T, Pr, key, on, pf);
                 if (live && !ok) f4 |= 1u << i;
                 if (live && ok && on) {
                     const float4 m = __ldg(a.map32 + key);
@@ -633,9 +634,9 @@ __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
 // Fallback passes of k_from_map_ix4, by tier: 0 the float32 tier, 1 the
 // double-float pointing (float32 spin factors and terms), 2 the exact
 // float64 pointing, each on the samples the previous tier left.
-template <int TIER>
+template <int P, int TIER>
 __global__ void __launch_bounds__(kBlock) k_from_map_ix_fix(GatherArgs a, MxMask mm) {
-    constexpr int C = SO3G_COORD_CAR, P = PX_FLAT_NT_NN;
+    constexpr int C = SO3G_COORD_CAR;
     const int nc = a.g.ncomp;
     mx_for_each<TIER < 2>(a.segs, a.piece, mm, [&](int det, int t) -> bool {
         const QuatD ofs = load_quat(a.dets + 4LL * det);
@@ -653,7 +654,8 @@ __global__ void __launch_bounds__(kBlock) k_from_map_ix_fix(GatherArgs a, MxMask
                 return false;
             if (on) {
                 float *sp = a.signal + det * a.sig_stride + t;
-                const float4 m = __ldg(a.map32 + (pix[0] * a.g.nx + pix[1]));
+                const float4 m = __ldg(a.map32 + (P == PX_HP_NT ? (long long)pix[0]
+                                                                : (long long)pix[0] * a.g.nx + pix[1]));
                 float sv = fmaf(m.x, pf[0], *sp);
                 if (nc > 1) sv = fmaf(m.y, pf[1], sv);
                 if (nc > 2) sv = fmaf(m.z, pf[2], sv);
@@ -670,23 +672,25 @@ __global__ void __launch_bounds__(kBlock) k_from_map_ix_fix(GatherArgs a, MxMask
     });
 }
 
+template <int P>
 struct GatherIxFix {
     const GatherArgs &a;
     const MxMask &mm;
     template <int T>
     void launch(unsigned nb, cudaStream_t st) const {
-        k_from_map_ix_fix<T><<<nb, kBlock, 0, st>>>(a, mm);
+        k_from_map_ix_fix<P, T><<<nb, kBlock, 0, st>>>(a, mm);
     }
 };
 
 // The chunked from_map for CAR maps with the untiled nearest-neighbour
-// pixelizor; returns 1 (nothing launched) where it does not apply.
+// pixelizor and for untiled HEALPix maps; returns 1 (nothing launched)
+// where it does not apply.
 template <int C, int P>
 int gather_interp(const GatherArgs &a, dim3 grid, cudaStream_t stream) {
-    if constexpr (!(C == SO3G_COORD_CAR && P == PX_FLAT_NT_NN)) {
+    if constexpr (!(C == SO3G_COORD_CAR && (P == PX_FLAT_NT_NN || P == PX_HP_NT))) {
         return 1;
     } else {
-        const long long npix = (long long)a.g.ny * a.g.nx;
+        const long long npix = P == PX_HP_NT ? a.g.npix : (long long)a.g.ny * a.g.nx;
         if (a.segs.seg || a.segs.n_time < 2 || !a.map32 || npix >= (1LL << 31) ||
             a.g.ncomp < 1 || a.g.ncomp > 3 || a.piece % kIxLen)
             return 1;
@@ -698,13 +702,14 @@ int gather_interp(const GatherArgs &a, dim3 grid, cudaStream_t stream) {
             return 1;
         }
         if (a.g.ncomp == 1)
-            k_from_map_ix4<1><<<grid, kBlock, 0, stream>>>(a, mm, ixb);
+            k_from_map_ix4<P, 1><<<grid, kBlock, 0, stream>>>(a, mm, ixb);
         else if (a.g.ncomp == 2)
-            k_from_map_ix4<2><<<grid, kBlock, 0, stream>>>(a, mm, ixb);
+            k_from_map_ix4<P, 2><<<grid, kBlock, 0, stream>>>(a, mm, ixb);
         else
-            k_from_map_ix4<3><<<grid, kBlock, 0, stream>>>(a, mm, ixb);
+            k_from_map_ix4<P, 3><<<grid, kBlock, 0, stream>>>(a, mm, ixb);
         int rc = after_launch("from_map (chunked)");
-        if (rc == SO3G_OK) rc = fix_tiers<0>(GatherIxFix{a, mm}, mm, stream, "from_map (chunked fallback)");
+        if (rc == SO3G_OK)
+            rc = fix_tiers<0>(GatherIxFix<P>{a, mm}, mm, stream, "from_map (chunked fallback)");
         cudaFreeAsync(mm.words, stream);
         cudaFreeAsync(ixb, stream);
         return rc;

@@ -60,15 +60,31 @@ struct IxBore {
 };
 
 // Per (detector, chunk): the model's coefficients and bounds, read by the
-// lanes of a chunk (five 16-byte words).
+// lanes of a chunk (six 16-byte words).
 struct __align__(16) IxParams {
     float xf, yf, b1, b2;       // x = xb + xf + s (b1 + s (b2 + s b3)) (pixels)
     float b3, e1, e2, e3;       // y = yb + yf + s (e1 + s (e2 + s e3))
-    float v0r, v0i, v1r, v1i;   // v = v0 + s v1 + s^2 v2
-    float v2r, v2i, hx, hy;     // 1/2 - bounds (pixels; < 0: not modelled)
-    float inv_len;              // 1 / (tb - ta)
-    int ta, xb, yb;             // chunk start; the anchor's integer parts
+    float v0r, v0i, v1r, v1i;   // v = v0 + s (v1 + s (v2 + s v3))
+    float v2r, v2i, hx, hy;     // hx, hy: 1/2 - bounds (pixels; < 0: not modelled)
+    float v3r, v3i, inv_len;    // inv_len = 1 / (tb - ta)
+    int ta;                     // chunk start
+    int xb, yb, pad0, pad1;     // the anchor's integer parts
 };
+
+// The same six words for a HEALPix map: the sample's phi (radians) and
+// z = sin(lat) as polynomials in s, with bounds on their errors against
+// the reference's float64 values; the pixel follows from them per sample
+// (hp_pixel_f32).
+struct __align__(16) IxParamsHp {
+    float lon_a, b1, b2, b3;    // lon = lon_a + s (b1 + s (b2 + s b3))
+    float z_a, z1, z2, elon;    // z = z_a + s (z1 + s (z2 + s z3)); elon < 0: not modelled
+    float v0r, v0i, v1r, v1i;   // v as IxParams
+    float v2r, v2i, ez, z3;
+    float v3r, v3i, inv_len;
+    int ta;
+    int pad0, pad1, pad2, pad3;
+};
+static_assert(sizeof(IxParamsHp) == sizeof(IxParams), "one shared-memory slot for both");
 
 // The chunks' boresight models (one thread per chunk), in float64.
 __global__ void k_ix_bore(const double *bore, int n_time, int n_chunks, IxBore *out) {
@@ -155,9 +171,10 @@ __device__ __forceinline__ void form_v2(const float (&p)[4], const float (&q)[4]
 
 // The model of chunk j for a detector (double-float qd, float32 q32): the
 // anchor from the certified double-float pointing, the coefficients and
-// bounds as described above.  Leaves hx = hy = -1 (every sample to the
-// fallback pass) where the model does not apply.
-template <class Args>
+// bounds as described above.  Leaves hx = hy = -1 (HP: elon = -1; every
+// sample to the fallback pass) where the model does not apply.  HP: the
+// HEALPix form (IxParamsHp) -- phi and z instead of pixel coordinates.
+template <bool HP, class Args>
 __device__ __forceinline__ void ix_setup(const Args &a, const IxBore *ixb, int j, int n_time,
                                          const dfl (&qd)[4], const float (&q32)[4],
                                          IxParams &p) {
@@ -170,20 +187,35 @@ __device__ __forceinline__ void ix_setup(const Args &a, const IxBore *ixb, int j
     }
     p.ta = ta;
     p.inv_len = tb > ta ? 1.f / (float)(tb - ta) : 0.f;
-    p.hx = p.hy = -1.f;
+    p.hx = p.hy = -1.f;   // HP: elon = z1 = -1 (the slot's third word of P1)
+    IxParamsHp &ph = reinterpret_cast<IxParamsHp &>(p);
+    if (HP) ph.elon = -1.f;
     const double2 lo = __ldg(reinterpret_cast<const double2 *>(a.bore + 4LL * ta));
     const double2 hi = __ldg(reinterpret_cast<const double2 *>(a.bore + 4LL * ta) + 1);
     dfl qb[4];
     if (!(df_split(lo.x, qb[0]) & df_split(lo.y, qb[1]) & df_split(hi.x, qb[2]) &
           df_split(hi.y, qb[3])))
         return;
-    dfl X, Y, Nc, Ns, D;
-    if (!fast_native<SO3G_COORD_CAR>(a.ft, a.fc, qb, qd, X, Y, Nc, Ns, D)) return;
-    const dfl xa = df_add(df_mul(X, a.fc.inv_cdx), a.fc.off_x);
-    const dfl ya = df_add(df_mul(Y, a.fc.inv_cdy), a.fc.off_y);
-    if (!(fabsf(xa.hi) < 1e7f && fabsf(ya.hi) < 1e7f)) return;
-    dfl fx, fy;
-    const int xb = df_floor(xa, fx), yb = df_floor(ya, fy);
+    // Anchor: CAR, the pixel coordinates (xb + fx, yb + fy); HEALPix, phi
+    // and z = sin(lat) (the quaternion's form; the reference's z is
+    // sin(ASIN(z)), within the table's error of it).
+    dfl X, fx{0.f, 0.f}, fy{0.f, 0.f}, za_df{0.f, 0.f};
+    int xb = 0, yb = 0;
+    if constexpr (!HP) {
+        dfl Y, Nc, Ns, D;
+        if (!fast_native<SO3G_COORD_CAR>(a.ft, a.fc, qb, qd, X, Y, Nc, Ns, D)) return;
+        const dfl xa = df_add(df_mul(X, a.fc.inv_cdx), a.fc.off_x);
+        const dfl ya = df_add(df_mul(Y, a.fc.inv_cdy), a.fc.off_y);
+        if (!(fabsf(xa.hi) < 1e7f && fabsf(ya.hi) < 1e7f)) return;
+        xb = df_floor(xa, fx);
+        yb = df_floor(ya, fy);
+    } else {
+        dfl qa_, qb_, qc_, qd_, Nc, Ns, D;
+        df_qmul(qb, qd, qa_, qb_, qc_, qd_);
+        za_df = df_dot<4>({qa_, qb_, qc_, qd_}, {qa_, df_neg(qb_), df_neg(qc_), qd_});
+        if (!(fabsf(za_df.hi) < 0.95f)) return;
+        if (!fast_lon_spin(a.ft, a.fc, qa_, qb_, qc_, qd_, za_df, X, Nc, Ns, D)) return;
+    }
 
     // The model quaternions, float32.
     const IxBore B = ixb[j];
@@ -205,47 +237,57 @@ __device__ __forceinline__ void ix_setup(const Args &a, const IxBore *ixb, int j
     // A1 and A2 within 9u of their norms (d1, d2 are the model's own).
     // Through the polar forms (|2B_w| <= sqrt2, |2B_Z| <= 2) and their
     // four-term sums: W1 within 33u n0 n1, W2 within 34u n0 n2 + 17u n1^2,
-    // Z1 within 46u n0 n1, Z2 within 47u n0 n2 + 23u n1^2.
-    const float ecoef = 48.f * u * (n0 * (n1 + n2) + n1 * n1);
+    // W3 within 31u n1 n2, Z1 within 46u n0 n1, Z2 within 47u n0 n2 + 23u
+    // n1^2, Z3 within 44u n1 n2.
+    const float ecoef = 48.f * u * (n0 * (n1 + n2) + n1 * (n1 + n2));
     // W0 and Z0 are evaluated from A0: W0 to 17u n0^2 (relative 17u n0^2 /
     // |W0| once divided out), Z0 to 24u n0^2 (moving the asin
     // coefficients).
     const float rel0 = 17.f * u * n0 * n0;
     const float dZ0 = 24.f * u * n0 * n0;
 
-    // Longitude: w(s) = W0 + W1 s + W2 s^2 (+ W3 s^3 + W4 s^4).
-    float w0x, w0y, w1x, w1y, w2x, w2y, t0x, t0y;
+    // Longitude: w(s) = W0 + W1 s + W2 s^2 + W3 s^3 (+ W4 s^4).
+    float w0x, w0y, w1x, w1y, w2x, w2y, w3x, w3y, t0x, t0y;
     form_w(A0, w0x, w0y);
     form_w2(A0, A1, w1x, w1y);
     form_w(A1, w2x, w2y);
     form_w2(A0, A2, t0x, t0y);
     w2x += t0x;
     w2y += t0y;
+    form_w2(A1, A2, w3x, w3y);
     const float w0a2 = w0x * w0x + w0y * w0y;
     const float w0a = sqrtf(w0a2);
     if (!(w0a > 0.1f)) return;                     // |sin lat| >~ 0.98
     const float ir = 1.f / w0a2;
     const float c1r = (w1x * w0x + w1y * w0y) * ir, c1i = (w1y * w0x - w1x * w0y) * ir;
     const float c2r = (w2x * w0x + w2y * w0y) * ir, c2i = (w2y * w0x - w2x * w0y) * ir;
+    const float c3r = (w3x * w0x + w3y * w0y) * ir, c3i = (w3y * w0x - w3x * w0y) * ir;
     const float s2 = 1.41421356f;
-    const float eta = (s2 * n1 * n2 + n2 * n2 / s2 + s2 * Em * E + E * E / s2) / w0a;
+    // Dropped: W4 = w(A2) (|w(q)| <= |q|^2 / sqrt2) and the model error E.
+    const float eta = (n2 * n2 / s2 + s2 * Em * E + E * E / s2) / w0a;
     const float c1a = sqrtf(c1r * c1r + c1i * c1i), c2a = sqrtf(c2r * c2r + c2i * c2i);
-    const float zmax = c1a + c2a + eta + ecoef / w0a;
+    const float c3a = sqrtf(c3r * c3r + c3i * c3i);
+    const float zmax = c1a + c2a + c3a + eta + ecoef / w0a;
     if (!(zmax < 0.05f)) return;
     const float dlmax = zmax * (1.f + zmax);
     // atan2 seam: lon stays inside (-pi, pi) over the chunk.
     if (!(fabsf(X.hi) + dlmax < 3.1405f)) return;
-    // Per sample the series Im(z - z^2/2 + z^3/3), z = c1 s + c2 s^2, is
-    // evaluated as its expansion in s cut after s^3 (pixels: x = xf +
-    // s (b1 + s (b2 + s b3))):
-    //   b1 = Im c1,  b2 = Im c2 - Im(c1^2)/2,  b3 = Im(c1^3)/3 - Im(c1 c2);
-    // the cut s^4..s^6 terms are within |c2| (|c1|^2 + |c1||c2| + |c2|^2/3
-    // + |c2|/2).
-    const float icxs = a.mc.inv_cdx, icys = a.mc.inv_cdy;
+    // Per sample the series Im(z - z^2/2 + z^3/3), z = c1 s + c2 s^2 +
+    // c3 s^3, is evaluated as its expansion in s cut after s^3 (pixels:
+    // x = xf + s (b1 + s (b2 + s b3))):
+    //   b1 = Im c1,  b2 = Im c2 - Im(c1^2)/2,
+    //   b3 = Im c3 - Im(c1 c2) + Im(c1^3)/3;
+    // the cut terms of z^2 / 2 and z^3 / 3 (those of degree >= 4 in s) are
+    // within (zc^2 - |c1|(|c1| + 2|c2|)) / 2 + (zc^3 - |c1|^3) / 3, zc =
+    // |c1| + |c2| + |c3|.
+    const float icxs = HP ? 1.f : a.mc.inv_cdx, icys = HP ? 1.f : a.mc.inv_cdy;
     const float b1 = c1i * icxs;
     const float b2 = (c2i - c1r * c1i) * icxs;
-    const float b3 = (c1i * (c1r * c1r - c1i * c1i * (1.f / 3.f)) - (c1r * c2i + c1i * c2r)) * icxs;
-    const float cut_lon = c2a * (c1a * (c1a + c2a) + c2a * (c2a * (1.f / 3.f) + 0.5f));
+    const float b3 = (c3i + c1i * (c1r * c1r - c1i * c1i * (1.f / 3.f)) -
+                      (c1r * c2i + c1i * c2r)) * icxs;
+    const float zc = c1a + c2a + c3a;
+    const float cut_lon = 0.5f * (zc * zc - c1a * (c1a + 2.f * c2a)) +
+                          (zc * zc * zc - c1a * c1a * c1a) * (1.f / 3.f);
     // Series remainder, the cut terms, the dropped terms (eta) and the
     // coefficients' errors through the series' derivative (<= 1 + 2|z|):
     // W1, W2's absolute errors, W0's relative error and the division's
@@ -261,15 +303,24 @@ __device__ __forceinline__ void ix_setup(const Args &a, const IxBore *ixb, int j
     // and of the per-sample Horner steps (4u of dlmax / cdelt, u of x).
     const float bx = 1.5f * (lon_err * icx + 1e-7f + 8.f * u * zmax * (1.f + zmax) * icx +
                              u * (4.f * dlmax * icx + 2.f));
+    // HEALPix: lon itself per sample (radians), lon_a + the cubic: lon_err,
+    // the anchor's float32 rounding (and double-float's 1e-12), b1..b3's
+    // roundings, the Horner steps and the final sum.
+    const float lon_a = X.hi + X.lo;
+    const float elon = lon_err + 8.f * u * zmax * (1.f + zmax) + 4.f * u * dlmax +
+                       2.f * u * (fabsf(lon_a) + dlmax) + 1e-12f;
 
-    // Latitude: Z(s) = Z0 + Z1 s + Z2 s^2 (+ Z3 s^3 + Z4 s^4).
+    // Latitude: Z(s) = Z0 + Z1 s + Z2 s^2 + Z3 s^3 (+ Z4 s^4).
     const float Z0 = form_z(A0);
     const float Z1 = form_z2(A0, A1);
     const float Z2 = form_z(A1) + form_z2(A0, A2);
-    const float etaZ = 2.f * n1 * n2 + n2 * n2 + 2.f * Em * E + E * E;
-    const float dzmax = fabsf(Z1) + fabsf(Z2) + etaZ + ecoef;
+    const float Z3 = form_z2(A1, A2);
+    // Dropped: Z4 = Z(A2) (|Z(q)| <= |q|^2) and the model error.
+    const float etaZ = n2 * n2 + 2.f * Em * E + E * E;
+    const float dzmax = fabsf(Z1) + fabsf(Z2) + fabsf(Z3) + etaZ + ecoef;
     const float Zm = fabsf(Z0) + dzmax + 1e-6f;
     if (!(Zm < 0.95f)) return;
+
     // asin's Taylor coefficients at Z0: asin' = (1-Z^2)^-1/2, asin'' =
     // Z (1-Z^2)^-3/2, asin''' = (1+2Z^2)(1-Z^2)^-5/2, asin'''' = Z (9+6Z^2)
     // (1-Z^2)^-7/2, all increasing in |Z|; their bounds at Zm.
@@ -287,16 +338,18 @@ __device__ __forceinline__ void ix_setup(const Args &a, const IxBore *ixb, int j
     // h = 1 / (kLutN - 1).
     const float h2_8 = 1.f / (8.f * 16383.f * 16383.f);
     const float dz2 = dzmax * dzmax;
-    // Per sample k1 dZ + k2 dZ^2 + k3 dZ^3, dZ = Z1 s + Z2 s^2, is evaluated
-    // as its expansion in s cut after s^3 (pixels: y = yf + s (e1 + s (e2
-    // + s e3))):  e1 = k1 Z1,  e2 = k1 Z2 + k2 Z1^2,  e3 = 2 k2 Z1 Z2 +
-    // k3 Z1^3;  the cut terms are within k2 Z2^2 + k3 |Z2| (3 Z1^2 + 3 |Z1
-    // Z2| + Z2^2).
-    const float Z1a = fabsf(Z1), Z2a = fabsf(Z2);
+    // Per sample k1 dZ + k2 dZ^2 + k3 dZ^3, dZ = Z1 s + Z2 s^2 + Z3 s^3,
+    // is evaluated as its expansion in s cut after s^3 (pixels: y = yf +
+    // s (e1 + s (e2 + s e3))):  e1 = k1 Z1,  e2 = k1 Z2 + k2 Z1^2,
+    // e3 = k1 Z3 + 2 k2 Z1 Z2 + k3 Z1^3;  the cut terms are within
+    // k2 (dc^2 - |Z1|(|Z1| + 2|Z2|)) + k3 (dc^3 - |Z1|^3), dc = |Z1| + |Z2|
+    // + |Z3|.
+    const float Z1a = fabsf(Z1), Z2a = fabsf(Z2), dc = Z1a + Z2a + fabsf(Z3);
     const float e1 = k1 * Z1 * icys;
     const float e2 = (k1 * Z2 + k2 * Z1 * Z1) * icys;
-    const float e3 = (2.f * k2 * Z1 * Z2 + k3 * Z1 * Z1 * Z1) * icys;
-    const float cut_lat = k2m * Z2a * Z2a + k3m * Z2a * (3.f * Z1a * (Z1a + Z2a) + Z2a * Z2a);
+    const float e3 = (k1 * Z3 + 2.f * k2 * Z1 * Z2 + k3 * Z1 * Z1 * Z1) * icys;
+    const float cut_lat =
+        k2m * (dc * dc - Z1a * (Z1a + 2.f * Z2a)) + k3m * (dc * dc * dc - Z1a * Z1a * Z1a);
     // Series remainder; the cut terms; dZ's errors through the series'
     // derivative; Z0's error through the coefficients (d k_n / dZ0 = (n + 1)
     // k_(n+1)); the roundings of k1..k3 and e1..e3 (32u |dlat|); the ASIN
@@ -308,18 +361,47 @@ __device__ __forceinline__ void ix_setup(const Args &a, const IxBore *ixb, int j
     // In pixels, with the float32 1/cdelt and the Horner steps.
     const float by = 1.5f * (lat_err * icy + 1e-7f + u * (4.f * dlatmax * icy + 2.f));
 
-    // Spin: v(s) = V0 + V1 s + V2 s^2; the dropped terms and the model
-    // error must stay below 1e-7 of |v| for the float32 contract.
-    float v0x, v0y, v1x, v1y, v2x, v2y;
+    // Spin: v(s) = V0 + V1 s + V2 s^2 + V3 s^3; the dropped V4 = v(A2) and
+    // the model error must stay below 1e-7 of |v| for the float32 contract.
+    float v0x, v0y, v1x, v1y, v2x, v2y, v3x, v3y;
     form_v(A0, v0x, v0y);
     form_v2(A0, A1, v1x, v1y);
     form_v(A1, v2x, v2y);
     form_v2(A0, A2, t0x, t0y);
     v2x += t0x;
     v2y += t0y;
+    form_v2(A1, A2, v3x, v3y);
     const float v0a = sqrtf(v0x * v0x + v0y * v0y);
-    if (!((s2 * n1 * n2 + n2 * n2 / s2 + s2 * Em * E + E * E / s2) < 1e-7f * v0a)) return;
+    if (!((n2 * n2 / s2 + s2 * Em * E + E * E / s2) < 1e-7f * v0a)) return;
 
+    if constexpr (HP) {
+        // z itself per sample, z_a + s (Z1 + s Z2): the dropped terms and
+        // coefficient errors (etaZ + ecoef), the reference's z =
+        // sin(ASIN(z)) against z (the ASIN table's h^2/8 max|asin''|,
+        // twice), the anchor's float32 rounding and the Horner steps.
+        const float z_a = za_df.hi + za_df.lo;
+        const float ez = etaZ + ecoef + 2.f * h2_8 * Zm * r3 + 1e-12f +
+                         u * (2.f * fabsf(z_a) + 5.f * dzmax);
+        ph.lon_a = lon_a;
+        ph.b1 = b1;
+        ph.b2 = b2;
+        ph.b3 = b3;
+        ph.z_a = z_a;
+        ph.z1 = Z1;
+        ph.z2 = Z2;
+        ph.z3 = Z3;
+        ph.v3r = v3x;
+        ph.v3i = v3y;
+        ph.v0r = v0x;
+        ph.v0i = v0y;
+        ph.v1r = v1x;
+        ph.v1i = v1y;
+        ph.v2r = v2x;
+        ph.v2i = v2y;
+        ph.ez = ez;
+        ph.elon = elon;
+        return;
+    }
     p.xf = fx.hi + fx.lo;
     p.yf = fy.hi + fy.lo;
     p.xb = xb;
@@ -336,6 +418,8 @@ __device__ __forceinline__ void ix_setup(const Args &a, const IxBore *ixb, int j
     p.v1i = v1y;
     p.v2r = v2x;
     p.v2i = v2y;
+    p.v3r = v3x;
+    p.v3i = v3y;
     p.hx = 0.5f - bx;
     p.hy = 0.5f - by;
 }
@@ -351,21 +435,21 @@ template <int NC>
 __device__ __forceinline__ bool ix_eval(const IxParams &p, float s, const DGeom &g, float T,
                                         float Pr, int &key, bool &on, float (&pf)[3]) {
     const float4 *w = reinterpret_cast<const float4 *>(&p);
-    const float4 P0 = w[0], P1 = w[1], P3 = w[3], P4 = w[4];
+    const float4 P0 = w[0], P1 = w[1], P3 = w[3], P5 = w[5];
     const float x = fmaf(s, fmaf(s, fmaf(s, P1.x, P0.w), P0.z), P0.x);
     const float y = fmaf(s, fmaf(s, fmaf(s, P1.w, P1.z), P1.y), P0.y);
     const float fxl = floorf(x), fyl = floorf(y);
     const bool ok = fabsf((x - fxl) - 0.5f) < P3.z && fabsf((y - fyl) - 0.5f) < P3.w;
-    const int ix = __float_as_int(P4.z) + (int)fxl, iy = __float_as_int(P4.w) + (int)fyl;
+    const int ix = __float_as_int(P5.x) + (int)fxl, iy = __float_as_int(P5.y) + (int)fyl;
     on = (unsigned)ix < (unsigned)g.nx && (unsigned)iy < (unsigned)g.ny;
     key = iy * g.nx + ix;
     if constexpr (NC == 1) {
         pf[0] = T;
         pf[1] = pf[2] = 0.f;
     } else {
-        const float4 P2 = w[2];
-        const float vr = fmaf(s, fmaf(s, P3.x, P2.z), P2.x);
-        const float vi = fmaf(s, fmaf(s, P3.y, P2.w), P2.y);
+        const float4 P2 = w[2], P4 = w[4];
+        const float vr = fmaf(s, fmaf(s, fmaf(s, P4.x, P3.x), P2.z), P2.x);
+        const float vi = fmaf(s, fmaf(s, fmaf(s, P4.y, P3.y), P2.w), P2.y);
         const float k = Pr * rcp_approx(fmaf(vr, vr, vi * vi));
         const float v1 = fmaf(vr, vr, -vi * vi) * k, v2 = 2.f * vr * vi * k;
         if constexpr (NC == 2) {
@@ -381,11 +465,59 @@ __device__ __forceinline__ bool ix_eval(const IxParams &p, float s, const DGeom 
     return ok;
 }
 
+// The HEALPix form of ix_eval (IxParamsHp): phi and z from their
+// polynomials, the pixel index (always on the map) from hp_pixel_f32.
+template <int NC>
+__device__ __forceinline__ bool ix_eval_hp(const IxParams &pr, float s, const DGeom &g, float T,
+                                           float Pr, int &key, float (&pf)[3]) {
+    const float4 *w = reinterpret_cast<const float4 *>(&pr);
+    const float4 P0 = w[0], P1 = w[1], P3 = w[3];
+    const float lon = fmaf(s, fmaf(s, fmaf(s, P0.w, P0.z), P0.y), P0.x);
+    const float z = fmaf(s, fmaf(s, fmaf(s, P3.w, P1.z), P1.y), P1.x);
+    int pix[1] = {0};
+    const bool ok =
+        P1.w >= 0.f && hp_pixel_f32<PX_HP_NT, false, true>(g, lon, P1.w, z, P3.z, 0.f, 0.f, pix);
+    key = pix[0];
+    if constexpr (NC == 1) {
+        pf[0] = T;
+        pf[1] = pf[2] = 0.f;
+    } else {
+        const float4 P2 = w[2], P4 = w[4];
+        const float vr = fmaf(s, fmaf(s, fmaf(s, P4.x, P3.x), P2.z), P2.x);
+        const float vi = fmaf(s, fmaf(s, fmaf(s, P4.y, P3.y), P2.w), P2.y);
+        const float k = Pr * rcp_approx(fmaf(vr, vr, vi * vi));
+        const float v1 = fmaf(vr, vr, -vi * vi) * k, v2 = 2.f * vr * vi * k;
+        if constexpr (NC == 2) {
+            pf[0] = v1;
+            pf[1] = v2;
+            pf[2] = 0.f;
+        } else {
+            pf[0] = T;
+            pf[1] = v1;
+            pf[2] = v2;
+        }
+    }
+    return ok;
+}
+
+// One sample of the chunked pointing for pixelizor P (CAR untiled nearest
+// or HEALPix untiled): ok (certified), key (map index), on, spin factors.
+template <int P, int NC>
+__device__ __forceinline__ bool ix_sample(const IxParams &p, float s, const DGeom &g, float T,
+                                          float Pr, int &key, bool &on, float (&pf)[3]) {
+    if constexpr (P == PX_HP_NT) {
+        on = true;
+        return ix_eval_hp<NC>(p, s, g, T, Pr, key, pf);
+    } else {
+        return ix_eval<NC>(p, s, g, T, Pr, key, on, pf);
+    }
+}
+
 // s of sample tq + i of a chunk: (float)(tq + i - ta) * inv_len, the
 // difference formed exactly (|tq - ta| < 2^24).
 __device__ __forceinline__ float ix_s(const IxParams &p, int tq, int i) {
     const float4 P4 = reinterpret_cast<const float4 *>(&p)[4];
-    return ((float)(tq - __float_as_int(P4.y)) + (float)i) * P4.x;
+    return ((float)(tq - __float_as_int(P4.w)) + (float)i) * P4.z;
 }
 
 // The boresight models of a call's chunks, in stream-ordered memory; NULL

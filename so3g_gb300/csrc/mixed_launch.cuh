@@ -216,7 +216,7 @@ __device__ __forceinline__ void ix_flush_run(int key, const int (&off)[NV], cons
 // four that one sample per lane needs, and a fraction of the L2 atomics.
 // Samples it cannot certify are marked in the mask (bit b of word w = lane
 // 8w + b/4, sample b % 4).
-template <bool WEIGHT, int NC>
+template <int P, bool WEIGHT, int NC>
 __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
     k_scatter_ix4(ScatterArgs a, MxMask mm, const IxBore *ixb) {
     __shared__ IxParams sp[kBlock / 32][32];
@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
     using V = IxValues<WEIGHT, NC>;
     constexpr int NV = V::NV;
     int off[NV];
-    V::offsets(a.g.ny * a.g.nx, off);
+    V::offsets(P == PX_HP_NT ? (int)a.g.npix : a.g.ny * a.g.nx, off);
     const float *sig = WEIGHT ? nullptr : a.signal + det * a.sig_stride;
     const bool vec = (reinterpret_cast<unsigned long long>(sig) & 15) == 0;
     unsigned *mwb = mm.words + ((long long)blockIdx.x * gridDim.y + blockIdx.y) * mm.wpp;
@@ -256,7 +256,8 @@ __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
         return r;
     };
     for (int g = j0 + warp * 32; g < j1; g += (kBlock / 32) * 32) {
-        if (g + lane < j1) ix_setup(a, ixb, g + lane, a.segs.n_time, qd, q32, sp[warp][lane]);
+        if (g + lane < j1)
+            ix_setup<P == PX_HP_NT>(a, ixb, g + lane, a.segs.n_time, qd, q32, sp[warp][lane]);
         __syncwarp();
         const int nch = min(32, j1 - g);
         const int rounds = (nch + 1) / 2;
@@ -281,7 +282,7 @@ __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
                 int kk = 0;
                 bool on = false;
                 float pf[3];
-                const bool ok = ix_eval<NC>(pp, ix_s(pp, tq, i), a.g, T, Pr, kk, on, pf);
+                const bool ok = ix_sample<P, NC>(pp, ix_s(pp, tq, i), a.g, T, Pr, kk, on, pf);
                 if (live && !ok) f4 |= 1u << i;
                 key[i] = (live && ok && on) ? kk : -1;
                 V::values(sg[i], pf, det_wt, v[i]);
@@ -332,14 +333,14 @@ __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
 // The fallback passes of k_scatter_ix4, by tier: 0 the float32 tier, 1 the
 // double-float pointing (float32 spin factors and terms), 2 the exact
 // float64 pointing, each on the samples the previous tier left.
-template <bool WEIGHT, int TIER>
+template <int P, bool WEIGHT, int TIER>
 __global__ void __launch_bounds__(kBlock) k_scatter_ix_fix(ScatterArgs a, MxMask mm) {
-    constexpr int C = SO3G_COORD_CAR, P = PX_FLAT_NT_NN;
+    constexpr int C = SO3G_COORD_CAR;
     constexpr int NV = WEIGHT ? 6 : 3;
     int mult[NV];
     const int nc = a.g.ncomp;
     const unsigned vmask = value_slots<WEIGHT>(nc, mult);
-    const long long plane = (long long)a.g.ny * a.g.nx;
+    const long long plane = P == PX_HP_NT ? a.g.npix : (long long)a.g.ny * a.g.nx;
     mx_for_each<TIER < 2>(a.segs, a.piece, mm, [&](int det, int t) -> bool {
         const float det_wt = a.det_weights ? __ldg(a.det_weights + det) : 1.f;
         const QuatD ofs = load_quat(a.dets + 4LL * det);
@@ -359,7 +360,8 @@ __global__ void __launch_bounds__(kBlock) k_scatter_ix_fix(ScatterArgs a, MxMask
                 const float sg = WEIGHT ? 0.f : __ldg(a.signal + det * a.sig_stride + t);
                 float v[NV];
                 tap_values<WEIGHT, NV, true>(sg, pf, 1.f, det_wt, v);
-                double *p = a.map + (pix[0] * a.g.nx + pix[1]);
+                double *p = a.map + (P == PX_HP_NT ? (long long)pix[0]
+                                                   : (long long)pix[0] * a.g.nx + pix[1]);
 #pragma unroll
                 for (int q = 0; q < NV; q++)
                     if ((vmask >> q) & 1u) atomicAdd(p + mult[q] * plane, f2d(v[q]));
@@ -375,13 +377,13 @@ __global__ void __launch_bounds__(kBlock) k_scatter_ix_fix(ScatterArgs a, MxMask
     });
 }
 
-template <bool WEIGHT>
+template <int P, bool WEIGHT>
 struct ScatterIxFix {
     const ScatterArgs &a;
     const MxMask &mm;
     template <int T>
     void launch(unsigned nb, cudaStream_t st) const {
-        k_scatter_ix_fix<WEIGHT, T><<<nb, kBlock, 0, st>>>(a, mm);
+        k_scatter_ix_fix<P, WEIGHT, T><<<nb, kBlock, 0, st>>>(a, mm);
     }
 };
 
@@ -396,15 +398,17 @@ struct ScatterMxFix {
 };
 
 // The chunked pointing for CAR maps with the untiled nearest-neighbour
-// pixelizor over whole detectors (no sample segments); returns 1 (nothing
-// launched) where it does not apply or an allocation fails.
+// pixelizor and for untiled HEALPix maps, over whole detectors (no sample
+// segments); returns 1 (nothing launched) where it does not apply or an
+// allocation fails.
 template <int C, int P, bool WEIGHT>
 int scatter_interp(const ScatterArgs &a, dim3 grid, cudaStream_t stream) {
-    if constexpr (!(C == SO3G_COORD_CAR && P == PX_FLAT_NT_NN)) {
+    if constexpr (!(C == SO3G_COORD_CAR && (P == PX_FLAT_NT_NN || P == PX_HP_NT))) {
         return 1;
     } else {
         // Map offsets (key + plane offset) in 32 bits.
-        const long long nc = a.g.ncomp, npix = (long long)a.g.ny * a.g.nx;
+        const long long nc = a.g.ncomp;
+        const long long npix = P == PX_HP_NT ? a.g.npix : (long long)a.g.ny * a.g.nx;
         if (a.segs.seg || a.segs.n_time < 2 || nc < 1 || nc > 3 ||
             (WEIGHT ? nc * nc : nc) * npix >= (1LL << 31) || a.piece % kIxLen)
             return 1;
@@ -416,14 +420,14 @@ int scatter_interp(const ScatterArgs &a, dim3 grid, cudaStream_t stream) {
             return 1;
         }
         if (nc == 1)
-            k_scatter_ix4<WEIGHT, 1><<<grid, kBlock, 0, stream>>>(a, mm, ixb);
+            k_scatter_ix4<P, WEIGHT, 1><<<grid, kBlock, 0, stream>>>(a, mm, ixb);
         else if (nc == 2)
-            k_scatter_ix4<WEIGHT, 2><<<grid, kBlock, 0, stream>>>(a, mm, ixb);
+            k_scatter_ix4<P, WEIGHT, 2><<<grid, kBlock, 0, stream>>>(a, mm, ixb);
         else
-            k_scatter_ix4<WEIGHT, 3><<<grid, kBlock, 0, stream>>>(a, mm, ixb);
+            k_scatter_ix4<P, WEIGHT, 3><<<grid, kBlock, 0, stream>>>(a, mm, ixb);
         int rc = after_launch(WEIGHT ? "to_weight_map (chunked)" : "to_map (chunked)");
         if (rc == SO3G_OK)
-            rc = fix_tiers<0>(ScatterIxFix<WEIGHT>{a, mm}, mm, stream,
+            rc = fix_tiers<0>(ScatterIxFix<P, WEIGHT>{a, mm}, mm, stream,
                               WEIGHT ? "to_weight_map (chunked fallback)"
                                      : "to_map (chunked fallback)");
         cudaFreeAsync(mm.words, stream);

@@ -370,30 +370,23 @@ __device__ __forceinline__ bool mixed_zen(const DGeom &g, const MixedConst &mc,
     return true;
 }
 
-// The float32 tier for HEALPix (Pixelizor_Healpix::GetPixels through
-// ang2pix, src/healpix_bare.c:46-78, 271-306): z = sin(lat) and s =
-// cos(lat) from __sincosf of the float32 latitude (absolute error
-// <= 2^-21.41 for |lat| <= pi), every integer decision certified against
-// the propagated error bound (x1.5 safety).  Returns false when the sample
-// must go to the double-float path; the pixel is always on the map.
-template <int P, bool SPIN, bool PARENT>
-__device__ __forceinline__ bool mixed_healpix(const DGeom &g, const FastTables &ft,
-                                              const MixedConst &mc, const float (&qb)[4],
-                                              const float (&qd)[4], int nc, float T, float Pr,
-                                              int *pix, float *pf) {
+// The HEALPix pixel (ang2pix, src/healpix_bare.c:46-78, 271-306) of a
+// sample from float32 phi = lon (error <= elon), z = sin(lat) (<= ez) and
+// s = cos(lat) (<= es), every integer decision certified against the
+// propagated error bound (x1.5 safety).  False when it is not certain (or
+// nside is beyond float's integers); the pixel is always on the map.
+// FROM_Z: s is not given; the caps' s / sqrt((1 + |z|) / 3) is formed as
+// sqrt(3 (1 - |z|)), the same quantity.
+template <int P, bool PARENT, bool FROM_Z = false>
+__device__ __forceinline__ bool hp_pixel_f32(const DGeom &g, float lon, float elon, float z,
+                                             float ez, float s, float es, int *pix) {
     const long long nside = g.nside;
     if (nside > (1LL << 20)) return false;
-    MixedLonLat o;
-    if (!mixed_lonlat(ft, mc, qb, qd, o)) return false;
     constexpr float m = 1.5f;
-    float z, s;
-    __sincosf(o.lat, &z, &s);
-    const float ez = fmaf(fabsf(s), o.elat, 3.8e-7f);
-    const float es = fmaf(fabsf(z), o.elat, 3.8e-7f);
     // x = phi / (2 pi), wrapped into [0, 1); tt = 4 x.
     constexpr float kInv2Pi = 0.15915494f;
-    float x = o.lon * kInv2Pi;
-    float ex = fmaf(o.elon, kInv2Pi, 2.f * kU * fabsf(x));
+    float x = lon * kInv2Pi;
+    float ex = fmaf(elon, kInv2Pi, 2.f * kU * fabsf(x));
     if (!(fabsf(x) > m * ex)) return false;
     if (x < 0.f) {
         x += 1.f;
@@ -428,11 +421,21 @@ __device__ __forceinline__ bool mixed_healpix(const DGeom &g, const FastTables &
         if (!floor_cert(tt, m * ett, ntt)) return false;
         if (ntt >= 4) ntt = 3;
         const float tp = tt - (float)ntt;
-        const float q = (1.f + za) * 0.33333334f;
-        const float eq = fmaf(ez, 0.33333334f, 3.f * kU * q);
-        const float sq = sqrtf(q);
-        const float tmp = s / sq;
-        const float etmp = fmaf(es + tmp * eq / (2.f * q), 1.f / sq, 3.f * kU * tmp);
+        float tmp, etmp;
+        if (FROM_Z) {
+            // 1 - za is exact (za > 1/2); 3 (1 - za) and the root rounded
+            // once each; |sqrt(a) - sqrt(b)| <= |a - b| / sqrt(a); the
+            // reciprocal's 2u inside the 1.000001.
+            const float w1 = 1.f - za;
+            tmp = sqrtf(3.f * w1);
+            etmp = fmaf(3.f * fmaf(kU, w1, ez) * 1.000001f, rcp_approx(tmp), kU * tmp) + 1e-15f;
+        } else {
+            const float q = (1.f + za) * 0.33333334f;
+            const float eq = fmaf(ez, 0.33333334f, 3.f * kU * q);
+            const float sq = sqrtf(q);
+            tmp = s / sq;
+            etmp = fmaf(es + tmp * eq / (2.f * q), 1.f / sq, 3.f * kU * tmp);
+        }
         const float jp = tp * tmp, jm = (1.f - tp) * tmp;
         const float ejp = m * fmaf(ett, tmp, fmaf(tp, etmp, kU * jp));
         const float ejm = m * fmaf(ett, tmp, fmaf(1.f - tp, etmp, 2.f * kU * jm));
@@ -464,6 +467,25 @@ __device__ __forceinline__ bool mixed_healpix(const DGeom &g, const FastTables &
     } else {
         hp_tile_split(g.nppt, ip, pix[0], pix[1]);
     }
+    return true;
+}
+
+// The float32 tier for HEALPix (Pixelizor_Healpix::GetPixels): z = sin(lat)
+// and s = cos(lat) from __sincosf of the float32 latitude (absolute error
+// <= 2^-21.41 for |lat| <= pi), then hp_pixel_f32.  Returns false when the
+// sample must go to the double-float path.
+template <int P, bool SPIN, bool PARENT>
+__device__ __forceinline__ bool mixed_healpix(const DGeom &g, const FastTables &ft,
+                                              const MixedConst &mc, const float (&qb)[4],
+                                              const float (&qd)[4], int nc, float T, float Pr,
+                                              int *pix, float *pf) {
+    MixedLonLat o;
+    if (!mixed_lonlat(ft, mc, qb, qd, o)) return false;
+    float z, s;
+    __sincosf(o.lat, &z, &s);
+    const float ez = fmaf(fabsf(s), o.elat, 3.8e-7f);
+    const float es = fmaf(fabsf(z), o.elat, 3.8e-7f);
+    if (!hp_pixel_f32<P, PARENT>(g, o.lon, o.elon, z, ez, s, es, pix)) return false;
     if (SPIN) mixed_spin(o, nc, T, Pr, pf);
     return true;
 }

@@ -117,18 +117,26 @@ def test_mixed_maps_within_tolerance(tiled):
         assert np.abs(a - b).max() <= 1e-6 * np.abs(a).max()
 
 
+@pytest.mark.parametrize("pixelization", ["car", "hp_ring", "hp_nest"])
 @pytest.mark.parametrize("ncomp", [1, 2, 3])
 @pytest.mark.parametrize("accum", [_abi.ACCUM_WARP_RUNS, _abi.ACCUM_ATOMIC])
-def test_mixed_to_map_layouts(ncomp, accum):
-    """The chunked CAR to_map / to_weight_map / from_map with signal rows
-    that are not 16-byte aligned (a column slice of a wider array), an odd
-    sample count (a partial last chunk and an odd chunk count per piece),
-    detector weights with zeros, every component count and both
-    accumulation modes, against the exact path."""
+def test_mixed_to_map_layouts(pixelization, ncomp, accum):
+    """The chunked to_map / to_weight_map / from_map (CAR untiled nearest,
+    HEALPix untiled) with signal rows that are not 16-byte aligned (a
+    column slice of a wider array), an odd sample count (a partial last
+    chunk and an odd chunk count per piece), detector weights with zeros,
+    every component count and both accumulation modes, against the exact
+    path.  The HEALPix scan crosses the belt / cap boundary (|z| = 2/3)."""
     import torch
+    from test_gpu_certified import _hp_engine
     n_det, n_time = 24, 30_001
-    Q, dets, resp, gamma, sig = synth.workload(n_det, n_time, seed=59, radius_deg=1.0)
-    p, eng = _engine((600, 600), ARCMIN, False, ncomp=ncomp)
+    if pixelization == "car":
+        Q, dets, resp, gamma, sig = synth.workload(n_det, n_time, seed=59, radius_deg=1.0)
+        p, eng = _engine((600, 600), ARCMIN, False, ncomp=ncomp)
+    else:
+        Q, dets, resp, gamma, sig = synth.workload(n_det, n_time, seed=59, radius_deg=3.0,
+                                                   el=41.5, throw=40., v_az=2.)
+        p, eng = _hp_engine(512, pixelization == "hp_nest", False, ncomp=ncomp)
     q = synth.native(p, Q)
     qd, dd, rd = (torch.from_numpy(x).cuda() for x in (q, dets, resp))
     wide = torch.zeros((n_det, n_time + 1), dtype=torch.float32, device="cuda")

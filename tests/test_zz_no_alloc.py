@@ -202,7 +202,9 @@ def test_noalloc_every_pointing_mode_against_oracle(orc, kind):
     """Each pointing mode twice in a row against the oracle (exact and
     certified: 1e-12 of the map's scale, the float64 summation order; mixed:
     float32 spin factors, 1e-6 of the scale) and against so3g_proj_to_map
-    in the same mode (1e-12)."""
+    in the same mode (1e-12; mixed: within the mixed tolerance, as
+    so3g_proj_to_map evaluates CAR pointing from its chunk models, the
+    no-allocation entry point per sample)."""
     from so3g_gb300 import _abi
     from helpers import Case, oracle_map
     lib = _abi.lib()
@@ -231,7 +233,8 @@ def test_noalloc_every_pointing_mode_against_oracle(orc, kind):
         c.eng.pointing = mode
         ref = c.eng.to_map(None, c.bore, c.dets, c.resp, c.signal, None, None)
         from helpers import stack_map
-        assert np.abs(got - stack_map(ref)).max() <= 1e-12 * scale, mode
+        same = 1e-12 if mode != _abi.POINTING_MIXED else 2 * tol
+        assert np.abs(got - stack_map(ref)).max() <= same * scale, mode
 
 
 def test_noalloc_read_error_after_call_without_host_err():
