@@ -240,6 +240,37 @@ __device__ __forceinline__ long long hp_hpd2pix(long long nside, bool nest, int 
     }
 }
 
+// hp_hpd2pix in 32-bit integers, for nside <= 8192 (every index, and
+// 2 jr (jr - 1) for jr <= 4 nside, below 2^31): the same steps.
+__device__ __forceinline__ int hp_spread_bits32(int v) {
+    unsigned r = (unsigned)v & 0xffffu;
+    r = (r ^ (r << 8)) & 0x00ff00ffu;
+    r = (r ^ (r << 4)) & 0x0f0f0f0fu;
+    r = (r ^ (r << 2)) & 0x33333333u;
+    r = (r ^ (r << 1)) & 0x55555555u;
+    return (int)r;
+}
+
+__device__ __forceinline__ int hp_hpd2pix32(int nside, bool nest, int f, int ix, int iy) {
+    if (nest) return f * nside * nside + hp_spread_bits32(ix) + (hp_spread_bits32(iy) << 1);
+    const int nl4 = 4 * nside;
+    int jr = hp_jrll(f) * nside - ix - iy - 1;
+    if (jr < nside) {
+        int jp = (hp_jpll(f) * jr + ix - iy + 1) / 2;
+        jp = (jp > nl4) ? jp - nl4 : ((jp < 1) ? jp + nl4 : jp);
+        return 2 * jr * (jr - 1) + jp - 1;
+    } else if (jr > 3 * nside) {
+        jr = nl4 - jr;
+        int jp = (hp_jpll(f) * jr + ix - iy + 1) / 2;
+        jp = (jp > nl4) ? jp - nl4 : ((jp < 1) ? jp + nl4 : jp);
+        return 12 * nside * nside - 2 * (jr + 1) * jr + jp - 1;
+    } else {
+        int jp = (hp_jpll(f) * nside + ix - iy + 1 + ((jr - nside) & 1)) / 2;
+        jp = (jp > nl4) ? jp - nl4 : ((jp < 1) ? jp + nl4 : jp);
+        return 2 * nside * (nside - 1) + (jr - nside) * nl4 + jp - 1;
+    }
+}
+
 // Returns the pixel, or -1 for a NaN/inf angle (the reference converts NaN
 // to an integer there, which is undefined).
 __device__ __forceinline__ long long hp_ang2pix(long long nside, bool nest, double theta,

@@ -394,7 +394,7 @@ __device__ __forceinline__ bool hp_pixel_f32(const DGeom &g, float lon, float el
     }
     const float tt = 4.f * x, ett = 4.f * ex;
     const float za = fabsf(z);
-    const float fn = (float)nside;
+    const float fn = (float)(int)nside;   // nside <= 2^20: a 32-bit conversion
     // za <= 2/3 (the float32 2/3 is within 2e-8 of the float64 constant).
     if (!(fabsf(za - 0.6666667f) > fmaf(m, ez, 3e-8f))) return false;
     int f, ix, iy;
@@ -460,7 +460,9 @@ __device__ __forceinline__ bool hp_pixel_f32(const DGeom &g, float lon, float el
               floor_cert(HY, fmaf(ehy, fn, kU * fabsf(HY)), iy)))
             return false;
     }
-    const long long ip = hp_hpd2pix(nside, P == PX_HP_T ? true : (g.nest != 0), f, ix, iy);
+    const bool nest = P == PX_HP_T ? true : (g.nest != 0);
+    const long long ip = nside <= 8192 ? (long long)hp_hpd2pix32((int)nside, nest, f, ix, iy)
+                                       : hp_hpd2pix(nside, nest, f, ix, iy);
     if (ip < 0 || ip >= g.npix) return false;
     if (P == PX_HP_NT || PARENT) {
         pix[0] = (int)ip;
