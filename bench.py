@@ -296,9 +296,10 @@ MEASURED_TRAFFIC_PER_SAMPLE = {
 # and the float64 FMA rate measured on a GB300 (1.6 lane-ops/clock/SM).
 FP64_OPS_PER_SAMPLE_TO_MAP = 1.018354e9 * 32 / 2e8
 FP64_LANE_OPS_PER_S = 5.0e11
-# The same for the Precomp kernels (ncu, 100 detectors x 1M samples).
-MEASURED_TRAFFIC_PRECOMP = {"to_map": (2.400763e9 + 3.709e6) / 1e8,
-                            "from_map": (2.406085e9 + 413.98e6) / 1e8}
+# The same for the Precomp kernels (ncu, 100 detectors x 1M samples; from_map:
+# k_pc_from_map4, the per-call map split's 0.17 GB left out).
+MEASURED_TRAFFIC_PRECOMP = {"to_map": (2.400758e9 + 3.643e6) / 1e8,
+                            "from_map": (2.401953e9 + 391.81e6) / 1e8}
 
 
 def algorithmic_bytes(c, op):
