@@ -303,6 +303,28 @@ __device__ __forceinline__ bool fast_native(const FastTables &ft, const FastCons
             const dfl r = df_mulf(df_recip(sq), 2.f);
             X = df_mul(u, r);
             Y = df_mul(v, r);
+        } else if (C == SO3G_COORD_ARC) {
+            // :284-326: h = sqrt(sc^2 + ss^2) (sc = a*c + b*d, ss = a*b -
+            // c*d), R = ASIN(2 h) / h, or pi / h - R where a^2 + d^2 <
+            // b^2 + c^2; X = ss R, Y = sc R.  The exact path takes the
+            // reference's series branch (h < 1e-8) and the neighbourhoods
+            // of its two decisions: h < 1e-6, |(a^2 + d^2) - (b^2 + c^2)| <=
+            // 1e-6, and 2 h near 1 (the table's end, theta near 90 deg).
+            if (!(n.hi > 1e-4f)) return false;
+            const dfl h2 = df_dot<2>({u, v}, {u, v});
+            if (!(h2.hi > 1e-12f)) return false;
+            const dfl s2 = df_dot<2>({b, c}, {b, c});
+            const dfl dcs = df_sub(n, s2);
+            if (!(fabsf(dcs.hi) > 1e-6f)) return false;
+            const float h0 = sqrtf(h2.hi);
+            const dfl h = fast_two_sum(h0, (fmaf(-h0, h0, h2.hi) + h2.lo) / (2.f * h0));
+            const dfl x2 = df_mulf(h, 2.f);
+            if (!(x2.hi < 0.998f)) return false;
+            const dfl ih = df_recip(h);
+            dfl R = df_mul(lut_df(ft.asin_t, x2), ih);
+            if (dcs.hi < 0.f) R = df_sub(df_mul(fc.pi, ih), R);
+            X = df_mul(u, R);
+            Y = df_mul(v, R);
         } else {
             // SIN, :337-364: X = 2u, Y = 2v.
             if (!(n.hi > 1e-4f)) return false;

@@ -31,7 +31,7 @@ template <int C, int P>
 struct FastEligible {
     static constexpr bool value =
         (C == SO3G_COORD_CAR || C == SO3G_COORD_TAN || C == SO3G_COORD_ZEA ||
-         C == SO3G_COORD_SIN) &&
+         C == SO3G_COORD_SIN || C == SO3G_COORD_ARC) &&
         (P == PX_FLAT_NT_NN || P == PX_FLAT_T_NN || P == PX_FLAT_NT_BL ||
          P == PX_FLAT_T_BL) ||
         (C == SO3G_COORD_CAR && (P == PX_HP_NT || P == PX_HP_T));

@@ -67,7 +67,7 @@ struct PixCert {
         (P == PX_HP_NT || P == PX_HP_T)
             ? C == SO3G_COORD_CAR
             : (C == SO3G_COORD_CAR || C == SO3G_COORD_TAN || C == SO3G_COORD_ZEA ||
-               C == SO3G_COORD_SIN);
+               C == SO3G_COORD_SIN || C == SO3G_COORD_ARC);
 };
 
 // GetPixel of one sample (and, with PROJ, its spin factors) through the

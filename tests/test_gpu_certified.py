@@ -179,7 +179,7 @@ def test_certified_seam_and_poles():
     _compare(eng2, q, dets, resp, False, 3)
 
 
-@pytest.mark.parametrize("proj", ["TAN", "ZEA", "SIN"])
+@pytest.mark.parametrize("proj", ["TAN", "ZEA", "SIN", "ARC"])
 @pytest.mark.parametrize("tiled", [False, True])
 def test_certified_zenithal_at_scale(proj, tiled):
     """Nearest-neighbour zenithal maps: every pixel index and spin factor
@@ -228,7 +228,7 @@ def _newton_step(pixel_xy, lon, lat, x_t, y_t, h):
     return lon + (j22 * ex - j12 * ey) / det, lat + (-j21 * ex + j11 * ey) / det
 
 
-@pytest.mark.parametrize("proj", ["TAN", "ZEA", "SIN"])
+@pytest.mark.parametrize("proj", ["TAN", "ZEA", "SIN", "ARC"])
 def test_certified_zenithal_edges(orc, proj):
     """Zenithal samples placed on pixel edges (and 1e-13 either side): the
     uncertain ones go to the exact path and all results stay equal."""

@@ -20,7 +20,7 @@ MODES = (_abi.POINTING_EXACT, _abi.POINTING_CERTIFIED, _abi.POINTING_MIXED)
 
 def _case(seed):
     rng = np.random.default_rng(1000 + seed)
-    kind = ["CAR", "TAN", "ZEA", "SIN", "HP"][seed % 5]
+    kind = ["CAR", "TAN", "ZEA", "SIN", "HP", "ARC"][seed % 6]
     el = float(rng.uniform(20., 75.))
     az0 = float(rng.uniform(0., 360.))
     n_det = 8
@@ -52,7 +52,7 @@ def _case(seed):
     return kind, eng, maps, q, dets, resp
 
 
-@pytest.mark.parametrize("seed", range(30))
+@pytest.mark.parametrize("seed", range(36))
 def test_random_geometry(gpulib, seed):
     import torch
     kind, eng, maps, q, dets, resp = _case(seed)
@@ -71,7 +71,7 @@ def test_random_geometry(gpulib, seed):
         assert np.abs(a - b).max() <= 2e-5
 
 
-@pytest.mark.parametrize("seed", range(0, 30, 3))
+@pytest.mark.parametrize("seed", range(0, 36, 3))
 def test_random_geometry_to_map(gpulib, seed):
     """to_map over the same random geometries: certified maps equal the
     float64 path's up to float64 summation order, mixed ones within 1e-6

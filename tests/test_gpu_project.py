@@ -33,11 +33,11 @@ MODES = [_abi.POINTING_EXACT, _abi.POINTING_CERTIFIED, _abi.POINTING_MIXED]
 
 def rtol_for(bil, mode, coord="CAR"):
     """Map/signal tolerance against the float64 oracle: mixed pointing on
-    CAR, TAN, ZEA and SIN maps evaluates spin factors, bilinear weights and
-    from_map terms in float32; certified bilinear weights are within one
+    CAR, TAN, ZEA, SIN and ARC maps evaluates spin factors, bilinear weights
+    and from_map terms in float32; certified bilinear weights are within one
     float32 ulp; every other case forms each float32 term as the reference
     does."""
-    if mode == _abi.POINTING_MIXED and coord in ("CAR", "TAN", "ZEA", "SIN") and not bil:
+    if mode == _abi.POINTING_MIXED and coord in ("CAR", "TAN", "ZEA", "SIN", "ARC") and not bil:
         return RTOL_MIXED
     if bil and mode != _abi.POINTING_EXACT:
         return RTOL_BILINEAR_CERTIFIED
