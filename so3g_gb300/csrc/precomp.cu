@@ -226,12 +226,6 @@ __global__ void __launch_bounds__(kBlock) k_pc_from_map(PcArgs a) {
 // load instructions per 4 samples instead of five per sample, so that the
 // memory system, not the load issue rate, sets the pace.
 
-// Groups of 4 consecutive samples a thread of k_pc_scatter4 takes per
-// iteration (its runs of equal pixels are merged across them).  One group
-// (56 registers, more resident warps) measured 14 % faster than two and
-// 30 % faster than four on a 1' CAR scan.
-constexpr int kPcGroups = 1;
-
 // The 4 samples' pixel pairs (iy, ix) and spin factors from sample index s
 // (a multiple of 4).
 template <int NC>
@@ -262,26 +256,97 @@ __device__ __forceinline__ long long pc_offset(const PcArgs &a, int iy, int ix, 
     return (long long)iy * a.nx + ix;
 }
 
-// The thread's 4 * kPcGroups consecutive samples often share a pixel (a scan crosses a
-// pixel in several samples): their float32 terms are summed in registers
-// with compensated (TwoSum) additions and each run of equal pixels is
-// flushed with one float64 atomic per value -- hi + lo added in float64,
-// which is the exact run sum to ~2^-46, so the map differs from the
-// per-sample sums only in float64 summation order.  The L2 atomic rate,
-// not HBM, bounds the per-sample form of this kernel.
-template <int NV>
-__device__ __forceinline__ void pc_flush(double *map, long long off, long long plane,
-                                         const int (&slot)[NV], const float (&hi)[NV],
-                                         const float (&lo)[NV]) {
+// Upper-triangle pair (i, j), j >= i, of value k of an NC-component
+// weight map (NC <= 3), in the order i = 0..NC-1, j = i..NC-1.
+template <int NC>
+__device__ constexpr int pair_i(int k) {
+    return NC == 3 ? (k < 3 ? 0 : (k < 5 ? 1 : 2)) : (NC == 2 ? (k < 2 ? 0 : 1) : 0);
+}
+template <int NC>
+__device__ constexpr int pair_j(int k) {
+    return NC == 3 ? (k < 3 ? k : (k < 5 ? k - 2 : 2)) : (NC == 2 ? (k < 2 ? k : 1) : 0);
+}
+
+// One run total (hi + lo, at most 3 values from value K0 on) added to the
+// map: plane c (to_map) or i * NC + j (to_weight_map); key < 0: nothing.
+// hi + lo is added in float64, the exact run sum to ~2^-46, so the map
+// differs from the per-sample sums only in float64 summation order.
+template <bool WEIGHT, int NC, int K0, int G>
+__device__ __forceinline__ void pc_flush_slot(double *map, int key, long long plane,
+                                              const float (&hi)[3], const float (&lo)[3]) {
+    if (key < 0) return;
+    double *p = map + key;
 #pragma unroll
-    for (int k = 0; k < NV; k++) {
-        double d = f2d(hi[k]);
-        if (lo[k] != 0.f) d += f2d(lo[k]);
-        atomicAdd(map + off + slot[k] * plane, d);
+    for (int c = 0; c < G; c++) {
+        const int k = K0 + c;
+        const int pl = WEIGHT ? pair_i<NC>(k) * NC + pair_j<NC>(k) : k;
+        double d = f2d(hi[c]);
+        if (lo[c] != 0.f) d += f2d(lo[c]);
+        atomicAdd(p + pl * plane, d);
     }
 }
 
-template <bool WEIGHT, int NC, int G = kPcGroups>
+// Values K0..K0+G-1 of a lane's four samples: the runs of equal pixels
+// among them summed right to left with compensated (TwoSum) additions,
+// packed into run slots 0..3 and flushed slot by slot, one pass per slot
+// taken only when some lane of the warp has that many runs.  A run is ~5
+// samples on a 1' scan, so a round of 128 samples takes ~2 passes of
+// atomics, where flushing each run as it ends took up to four divergent
+// ones that touched the same sectors again (1000 det x 1M, 3x2000x2000:
+// to_map 5.64 -> 4.70 ms).
+template <bool WEIGHT, int NC, int K0, int G>
+__device__ __forceinline__ void pc_runs4(double *map, long long plane, const int (&key)[4],
+                                         const float (&sig)[4], const float (&f)[4 * NC],
+                                         float det_wt) {
+    float v[4][3], lo[4][3];
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const int k = K0 + c;
+            const float *pf = f + NC * j;
+            if (c >= G) v[j][c] = 0.f;
+            else if (WEIGHT) v[j][c] = pf[pair_i<NC>(k)] * pf[pair_j<NC>(k)] * det_wt;  // src/Projection.cxx:2151
+            else v[j][c] = det_wt * sig[j] * pf[k];  // src/Projection.cxx:2117
+            lo[j][c] = 0.f;
+        }
+    const bool h1 = key[1] != key[0], h2 = key[2] != key[1], h3 = key[3] != key[2];
+#pragma unroll
+    for (int c = 0; c < G; c++) {
+        float e;
+        if (!h3) { two_sum(v[2][c], v[3][c], v[2][c], e); lo[2][c] = e; }
+        if (!h2) { two_sum(v[1][c], v[2][c], v[1][c], e); lo[1][c] = lo[2][c] + e; }
+        if (!h1) { two_sum(v[0][c], v[1][c], v[0][c], e); lo[0][c] = lo[1][c] + e; }
+    }
+    // Slots 1 and 2: the first and second heads among samples 1..3; slot
+    // 3: sample 3 when all three are heads.
+    const int nruns = 1 + h1 + h2 + h3;
+    float s1[3], l1[3], s2[3], l2[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        s1[c] = h1 ? v[1][c] : (h2 ? v[2][c] : v[3][c]);
+        l1[c] = h1 ? lo[1][c] : (h2 ? lo[2][c] : lo[3][c]);
+        s2[c] = (h1 && h2) ? v[2][c] : v[3][c];
+        l2[c] = (h1 && h2) ? lo[2][c] : lo[3][c];
+    }
+    const int k1 = h1 ? key[1] : (h2 ? key[2] : key[3]);
+    const int k2 = (h1 && h2) ? key[2] : key[3];
+    pc_flush_slot<WEIGHT, NC, K0, G>(map, key[0], plane, v[0], lo[0]);
+    if (__any_sync(kFull, nruns > 1) && nruns > 1)
+        pc_flush_slot<WEIGHT, NC, K0, G>(map, k1, plane, s1, l1);
+    if (__any_sync(kFull, nruns > 2) && nruns > 2)
+        pc_flush_slot<WEIGHT, NC, K0, G>(map, k2, plane, s2, l2);
+    if (__any_sync(kFull, nruns > 3) && nruns > 3)
+        pc_flush_slot<WEIGHT, NC, K0, G>(map, key[3], plane, v[3], lo[3]);
+}
+
+// ProjEng_Precomp::to_map / to_weight_map (src/Projection.cxx:2084-2158)
+// with 4 consecutive samples per lane (a warp takes 128): the pixel pairs
+// as two int4, the spin factors as NC float4 and the signal as one float4.
+// The map's element offsets within a plane are 32-bit (the launcher takes
+// this kernel for planes below 2^31 pixels).  The values of a weight map are
+// summed in groups of three, which keeps them in registers.
+template <bool WEIGHT, int NC>
 __global__ void __launch_bounds__(kBlock) k_pc_scatter4(PcArgs a) {
     constexpr int NV = WEIGHT ? NC * (NC + 1) / 2 : NC;
     int det, t0, t1;
@@ -292,73 +357,30 @@ __global__ void __launch_bounds__(kBlock) k_pc_scatter4(PcArgs a) {
         if (det_wt == 0.f) return;  // src/Projection.cxx:2101-2105
     }
     const long long plane = (long long)a.ny * a.nx;
-    // Value k goes to map plane slot[k]: component c (to_map) or the
-    // upper-triangle pair (i, j), j >= i, at i * NC + j (to_weight_map).
-    int slot[NV];
-    {
-        int k = 0;
-        if (!WEIGHT) {
+    const int lane = threadIdx.x & 31;
+    // t1 - t0 is a multiple of 4: a lane's samples are all in or all out.
+    for (int tb = t0 + 128 * (threadIdx.x >> 5); tb < t1; tb += 4 * blockDim.x) {
+        const int tq = tb + 4 * lane;
+        int key[4] = {-1, -1, -1, -1};
+        float sig[4] = {0.f, 0.f, 0.f, 0.f};
+        float f[4 * NC];
 #pragma unroll
-            for (int c = 0; c < NC; c++) slot[k++] = c;
-        } else {
-#pragma unroll
-            for (int i = 0; i < NC; i++)
-#pragma unroll
-                for (int j = i; j < NC; j++) slot[k++] = i * NC + j;
-        }
-    }
-    for (int t = t0 + 4 * G * threadIdx.x; t < t1; t += 4 * G * blockDim.x) {
-        long long cur = -1;
-        float hi[NV], lo[NV];
-#pragma unroll
-        for (int g = 0; g < G; g++) {
-            const int tg = t + 4 * g;
-            if (tg >= t1) break;   // t1 - t0 is a multiple of 4 only
-            const long long s = (long long)det * a.n_time + tg;
+        for (int k = 0; k < 4 * NC; k++) f[k] = 0.f;
+        if (tq < t1) {
+            const long long s = (long long)det * a.n_time + tq;
             int p[8];
-            float f[4 * NC];
             pc_load4<NC>(a, s, p, f);
-            float4 sg = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (!WEIGHT)
-                sg = __ldg(reinterpret_cast<const float4 *>(a.signal + det * a.sig_stride + tg));
-            const float sig[4] = {sg.x, sg.y, sg.z, sg.w};
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-                const long long off = pc_offset(a, p[2 * j], p[2 * j + 1], det, tg + j);
-                if (off < 0) continue;
-                const float *pf = f + NC * j;
-                float v[NV];
-                if (!WEIGHT) {
-                    // src/Projection.cxx:2117
-#pragma unroll
-                    for (int c = 0; c < NC; c++) v[c] = det_wt * sig[j] * pf[c];
-                } else {
-                    // src/Projection.cxx:2151
-                    int k = 0;
-#pragma unroll
-                    for (int i = 0; i < NC; i++)
-#pragma unroll
-                        for (int m = i; m < NC; m++) v[k++] = pf[i] * pf[m] * det_wt;
-                }
-                if (off == cur) {
-#pragma unroll
-                    for (int k = 0; k < NV; k++) {
-                        float e;
-                        two_sum(hi[k], v[k], hi[k], e);
-                        lo[k] += e;
-                    }
-                } else {
-                    if (cur >= 0) pc_flush<NV>(a.map, cur, plane, slot, hi, lo);
-                    cur = off;
-#pragma unroll
-                    for (int k = 0; k < NV; k++) {
-                        hi[k] = v[k];
-                        lo[k] = 0.f;
-                    }
-                }
+            if (!WEIGHT) {
+                const float4 sg =
+                    __ldg(reinterpret_cast<const float4 *>(a.signal + det * a.sig_stride + tq));
+                sig[0] = sg.x; sig[1] = sg.y; sig[2] = sg.z; sig[3] = sg.w;
             }
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                key[j] = (int)pc_offset(a, p[2 * j], p[2 * j + 1], det, tq + j);
         }
-        if (cur >= 0) pc_flush<NV>(a.map, cur, plane, slot, hi, lo);
+        pc_runs4<WEIGHT, NC, 0, (NV < 3 ? NV : 3)>(a.map, plane, key, sig, f, det_wt);
+        if constexpr (NV > 3) pc_runs4<WEIGHT, NC, 3, NV - 3>(a.map, plane, key, sig, f, det_wt);
     }
 }
 
@@ -480,6 +502,7 @@ __global__ void __launch_bounds__(kBlock, SPLIT ? 6 : 8)
 bool pc_vec_ok(const PcArgs &a, const void *sig, long long sig_stride, bool whole_rows) {
     auto al = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
     return !a.tiled && whole_rows && (a.n_time % 4) == 0 && al(a.pixel) && al(a.spin) &&
+           (long long)a.ny * a.nx <= 0x7fffffffLL &&
            (!sig || (al(sig) && (sig_stride % 4) == 0));
 }
 
