@@ -566,10 +566,12 @@ __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
     const bool vec = (reinterpret_cast<unsigned long long>(sig) & 15) == 0;
     unsigned *mwb = mm.words + ((long long)blockIdx.x * gridDim.y + blockIdx.y) * mm.wpp;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tsh = P == PX_HP_T ? __ffsll(a.g.nppt) - 1 : 0;
     const int j0 = t0 / kIxLen, j1 = (t1 - 1) / kIxLen + 1;
     for (int g = j0 + warp * 32; g < j1; g += (kBlock / 32) * 32) {
         if (g + lane < j1)
-            ix_setup<P == PX_HP_NT>(a, ixb, g + lane, a.segs.n_time, qd, q32, sp[warp][lane]);
+            ix_setup<P == PX_HP_NT || P == PX_HP_T>(a, ixb, g + lane, a.segs.n_time, qd, q32,
+                                                    sp[warp][lane]);
         __syncwarp();
         const int nch = min(32, j1 - g);
         const int rounds = (nch + 1) / 2;
@@ -603,12 +605,18 @@ __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
                 const bool ok = ix_sample<P, NC>(pp, ix_s(pp, tq, i), a.g, T, Pr, key, on, pf);
                 if (live && !ok) f4 |= 1u << i;
                 if (live && ok && on) {
+                    // Tiled: the float32 copy spans the parent map, .w = 0
+                    // on the pixels of absent tiles.
                     const float4 m = __ldg(a.map32 + key);
-                    // float32 terms (the mixed-precision contract).
-                    float x = fmaf(m.x, pf[0], sv[i]);
-                    if constexpr (NC > 1) x = fmaf(m.y, pf[1], x);
-                    if constexpr (NC > 2) x = fmaf(m.z, pf[2], x);
-                    sv[i] = x;
+                    if (P == PX_HP_T && m.w == 0.f) {
+                        record_missing_tile(a.err, key >> tsh);
+                    } else {
+                        // float32 terms (the mixed-precision contract).
+                        float x = fmaf(m.x, pf[0], sv[i]);
+                        if constexpr (NC > 1) x = fmaf(m.y, pf[1], x);
+                        if constexpr (NC > 2) x = fmaf(m.z, pf[2], x);
+                        sv[i] = x;
+                    }
                 }
             }
             if (__any_sync(kFull, f4 != 0u)) {
@@ -646,16 +654,25 @@ __global__ void __launch_bounds__(kBlock) k_from_map_ix_fix(GatherArgs a, MxMask
                                   d2f_round(ofs.d)};
             float qb[4];
             load_bore_f32(a.bore32, a.bore, t, qb);
+            // Tiled HEALPix: the parent map's NEST index (the float32
+            // copy's index, .w = 0 on absent tiles).
             int pix[2];
             float pf[3] = {0.f, 0.f, 0.f};
             bool on = false;
-            if (!mixed_pointing<C, P, true, false>(a.g, a.ft, a.mc, qb, q32, nc, T, Pr, pix, on,
-                                                   pf))
+            if (!mixed_pointing<C, P, true, P == PX_HP_T>(a.g, a.ft, a.mc, qb, q32, nc, T, Pr,
+                                                          pix, on, pf))
                 return false;
             if (on) {
                 float *sp = a.signal + det * a.sig_stride + t;
-                const float4 m = __ldg(a.map32 + (P == PX_HP_NT ? (long long)pix[0]
-                                                                : (long long)pix[0] * a.g.nx + pix[1]));
+                const float4 m =
+                    __ldg(a.map32 + (P == PX_FLAT_NT_NN ? (long long)pix[0] * a.g.nx + pix[1]
+                                                        : (long long)pix[0]));
+                if (P == PX_HP_T && m.w == 0.f) {
+                    int tp[3];
+                    parent_to_tile<P>(a.g, pix, tp);
+                    record_missing_tile(a.err, tp[0]);
+                    return true;
+                }
                 float sv = fmaf(m.x, pf[0], *sp);
                 if (nc > 1) sv = fmaf(m.y, pf[1], sv);
                 if (nc > 2) sv = fmaf(m.z, pf[2], sv);
@@ -683,14 +700,15 @@ struct GatherIxFix {
 };
 
 // The chunked from_map for CAR maps with the untiled nearest-neighbour
-// pixelizor and for untiled HEALPix maps; returns 1 (nothing launched)
-// where it does not apply.
+// pixelizor and for HEALPix maps (untiled or tiled: the float32 copy spans
+// the parent map); returns 1 (nothing launched) where it does not apply.
 template <int C, int P>
 int gather_interp(const GatherArgs &a, dim3 grid, cudaStream_t stream) {
-    if constexpr (!(C == SO3G_COORD_CAR && (P == PX_FLAT_NT_NN || P == PX_HP_NT))) {
+    if constexpr (!(C == SO3G_COORD_CAR &&
+                    (P == PX_FLAT_NT_NN || P == PX_HP_NT || P == PX_HP_T))) {
         return 1;
     } else {
-        const long long npix = P == PX_HP_NT ? a.g.npix : (long long)a.g.ny * a.g.nx;
+        const long long npix = P == PX_FLAT_NT_NN ? (long long)a.g.ny * a.g.nx : a.g.npix;
         if (a.segs.seg || a.segs.n_time < 2 || !a.map32 || npix >= (1LL << 31) ||
             a.g.ncomp < 1 || a.g.ncomp > 3 || a.piece % kIxLen)
             return 1;
@@ -722,11 +740,11 @@ int gather_interp(const GatherArgs &a, dim3 grid, cudaStream_t stream) {
 // allocated.
 template <int C, int P>
 int gather_mixed(const GatherArgs &a, dim3 grid, cudaStream_t stream) {
+    const int ri = gather_interp<C, P>(a, grid, stream);
+    if (ri != 1) return ri;
     if constexpr (!MxEligible<C, P>::value) {
         return 1;
     } else {
-        const int ri = gather_interp<C, P>(a, grid, stream);
-        if (ri != 1) return ri;
         const long long npix = P == PX_HP_NT ? a.g.npix : (long long)a.g.ny * a.g.nx;
         if (!a.bore32 || !a.map32 || npix >= (1LL << 31)) return 1;
         MxMask mm;

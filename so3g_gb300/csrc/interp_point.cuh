@@ -466,8 +466,9 @@ __device__ __forceinline__ bool ix_eval(const IxParams &p, float s, const DGeom 
 }
 
 // The HEALPix form of ix_eval (IxParamsHp): phi and z from their
-// polynomials, the pixel index (always on the map) from hp_pixel_f32.
-template <int NC>
+// polynomials, the pixel index (always on the map) from hp_pixel_f32 --
+// for a tiled map (P = PX_HP_T) the parent map's NEST index.
+template <int P, int NC>
 __device__ __forceinline__ bool ix_eval_hp(const IxParams &pr, float s, const DGeom &g, float T,
                                            float Pr, int &key, float (&pf)[3]) {
     const float4 *w = reinterpret_cast<const float4 *>(&pr);
@@ -476,7 +477,7 @@ __device__ __forceinline__ bool ix_eval_hp(const IxParams &pr, float s, const DG
     const float z = fmaf(s, fmaf(s, fmaf(s, P3.w, P1.z), P1.y), P1.x);
     int pix[1] = {0};
     const bool ok =
-        P1.w >= 0.f && hp_pixel_f32<PX_HP_NT, false, true>(g, lon, P1.w, z, P3.z, 0.f, 0.f, pix);
+        P1.w >= 0.f && hp_pixel_f32<P, P == PX_HP_T, true>(g, lon, P1.w, z, P3.z, 0.f, 0.f, pix);
     key = pix[0];
     if constexpr (NC == 1) {
         pf[0] = T;
@@ -501,13 +502,14 @@ __device__ __forceinline__ bool ix_eval_hp(const IxParams &pr, float s, const DG
 }
 
 // One sample of the chunked pointing for pixelizor P (CAR untiled nearest
-// or HEALPix untiled): ok (certified), key (map index), on, spin factors.
+// or HEALPix): ok (certified), key (map index; tiled HEALPix: the parent
+// map's NEST index), on, spin factors.
 template <int P, int NC>
 __device__ __forceinline__ bool ix_sample(const IxParams &p, float s, const DGeom &g, float T,
                                           float Pr, int &key, bool &on, float (&pf)[3]) {
-    if constexpr (P == PX_HP_NT) {
+    if constexpr (P == PX_HP_NT || P == PX_HP_T) {
         on = true;
-        return ix_eval_hp<NC>(p, s, g, T, Pr, key, pf);
+        return ix_eval_hp<P, NC>(p, s, g, T, Pr, key, pf);
     } else {
         return ix_eval<NC>(p, s, g, T, Pr, key, on, pf);
     }

@@ -194,13 +194,35 @@ struct IxValues {
     }
 };
 
-// One run total of k_scatter_ix4 added to the map (key < 0: nothing).
-template <int NV>
-__device__ __forceinline__ void ix_flush_run(int key, const int (&off)[NV], const float (&v)[NV],
-                                             double *map) {
-    if (key >= 0) {
+// Map element of a chunked sample's key (key < 0: none): key itself on an
+// untiled map; on a tiled HEALPix map (key = the parent NEST index) the
+// element of its tile (tile = key >> tsh, tsh = log2 of the pixels per
+// tile), NULL with the missing-tile error recorded when the tile is absent.
+template <int P>
+__device__ __forceinline__ double *ix_base(const ScatterArgs &a, int key, int tsh) {
+    if (key < 0) return nullptr;
+    if constexpr (P != PX_HP_T) {
+        return a.map + key;
+    } else {
+        const int tile = key >> tsh;
+        const long long toff = __ldg(a.g.tile_offset + tile);
+        if (toff < 0) {
+            record_missing_tile(a.err, tile);
+            return nullptr;
+        }
+        return a.map + toff + (key & ((1 << tsh) - 1));
+    }
+}
+
+// One run total of k_scatter_ix4 added to the map (key < 0: nothing); off
+// holds the values' plane offsets within the map (or the tile).
+template <int P, int NV>
+__device__ __forceinline__ void ix_flush_run(const ScatterArgs &a, int key, int tsh,
+                                             const int (&off)[NV], const float (&v)[NV]) {
+    double *p = ix_base<P>(a, key, tsh);
+    if (p) {
 #pragma unroll
-        for (int k = 0; k < NV; k++) atomicAdd(map + (key + off[k]), f2d(v[k]));
+        for (int k = 0; k < NV; k++) atomicAdd(p + off[k], f2d(v[k]));
     }
 }
 
@@ -235,7 +257,9 @@ __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
     using V = IxValues<WEIGHT, NC>;
     constexpr int NV = V::NV;
     int off[NV];
-    V::offsets(P == PX_HP_NT ? (int)a.g.npix : a.g.ny * a.g.nx, off);
+    V::offsets(P == PX_HP_NT ? (int)a.g.npix : (P == PX_HP_T ? (int)a.g.nppt : a.g.ny * a.g.nx),
+               off);
+    const int tsh = P == PX_HP_T ? __ffsll(a.g.nppt) - 1 : 0;
     const float *sig = WEIGHT ? nullptr : a.signal + det * a.sig_stride;
     const bool vec = (reinterpret_cast<unsigned long long>(sig) & 15) == 0;
     unsigned *mwb = mm.words + ((long long)blockIdx.x * gridDim.y + blockIdx.y) * mm.wpp;
@@ -257,7 +281,8 @@ __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
     };
     for (int g = j0 + warp * 32; g < j1; g += (kBlock / 32) * 32) {
         if (g + lane < j1)
-            ix_setup<P == PX_HP_NT>(a, ixb, g + lane, a.segs.n_time, qd, q32, sp[warp][lane]);
+            ix_setup<P == PX_HP_NT || P == PX_HP_T>(a, ixb, g + lane, a.segs.n_time, qd, q32,
+                                                    sp[warp][lane]);
         __syncwarp();
         const int nch = min(32, j1 - g);
         const int rounds = (nch + 1) / 2;
@@ -297,7 +322,7 @@ __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
             }
             if (a.accum != SO3G_ACCUM_WARP_RUNS) {
 #pragma unroll
-                for (int i = 0; i < 4; i++) ix_flush_run<NV>(key[i], off, v[i], a.map);
+                for (int i = 0; i < 4; i++) ix_flush_run<P, NV>(a, key[i], tsh, off, v[i]);
                 continue;
             }
             // Run heads and right-to-left run totals (in place: v[i] becomes
@@ -321,10 +346,11 @@ __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
             }
             ks1 = h1 ? key[1] : (h2 ? key[2] : key[3]);
             ks2 = (h1 && h2) ? key[2] : key[3];
-            ix_flush_run<NV>(key[0], off, v[0], a.map);
-            if (__any_sync(kFull, nruns > 1) && nruns > 1) ix_flush_run<NV>(ks1, off, s1, a.map);
-            if (__any_sync(kFull, nruns > 2) && nruns > 2) ix_flush_run<NV>(ks2, off, s2, a.map);
-            if (__any_sync(kFull, nruns > 3) && nruns > 3) ix_flush_run<NV>(key[3], off, v[3], a.map);
+            ix_flush_run<P, NV>(a, key[0], tsh, off, v[0]);
+            if (__any_sync(kFull, nruns > 1) && nruns > 1) ix_flush_run<P, NV>(a, ks1, tsh, off, s1);
+            if (__any_sync(kFull, nruns > 2) && nruns > 2) ix_flush_run<P, NV>(a, ks2, tsh, off, s2);
+            if (__any_sync(kFull, nruns > 3) && nruns > 3)
+                ix_flush_run<P, NV>(a, key[3], tsh, off, v[3]);
         }
         __syncwarp();
     }
@@ -340,7 +366,6 @@ __global__ void __launch_bounds__(kBlock) k_scatter_ix_fix(ScatterArgs a, MxMask
     int mult[NV];
     const int nc = a.g.ncomp;
     const unsigned vmask = value_slots<WEIGHT>(nc, mult);
-    const long long plane = P == PX_HP_NT ? a.g.npix : (long long)a.g.ny * a.g.nx;
     mx_for_each<TIER < 2>(a.segs, a.piece, mm, [&](int det, int t) -> bool {
         const float det_wt = a.det_weights ? __ldg(a.det_weights + det) : 1.f;
         const QuatD ofs = load_quat(a.dets + 4LL * det);
@@ -357,14 +382,18 @@ __global__ void __launch_bounds__(kBlock) k_scatter_ix_fix(ScatterArgs a, MxMask
                                                    pf))
                 return false;
             if (on) {
+                long long off, plane;
+                const int bad = locate<P>(a.g, pix, &off, &plane);
+                if (bad >= 0) {
+                    record_missing_tile(a.err, bad);
+                    return true;
+                }
                 const float sg = WEIGHT ? 0.f : __ldg(a.signal + det * a.sig_stride + t);
                 float v[NV];
                 tap_values<WEIGHT, NV, true>(sg, pf, 1.f, det_wt, v);
-                double *p = a.map + (P == PX_HP_NT ? (long long)pix[0]
-                                                   : (long long)pix[0] * a.g.nx + pix[1]);
 #pragma unroll
                 for (int q = 0; q < NV; q++)
-                    if ((vmask >> q) & 1u) atomicAdd(p + mult[q] * plane, f2d(v[q]));
+                    if ((vmask >> q) & 1u) atomicAdd(a.map + off + mult[q] * plane, f2d(v[q]));
             }
             return true;
         } else if constexpr (TIER == 1) {
@@ -398,17 +427,19 @@ struct ScatterMxFix {
 };
 
 // The chunked pointing for CAR maps with the untiled nearest-neighbour
-// pixelizor and for untiled HEALPix maps, over whole detectors (no sample
-// segments); returns 1 (nothing launched) where it does not apply or an
-// allocation fails.
+// pixelizor and for HEALPix maps (untiled or tiled), over whole detectors
+// (no sample segments); returns 1 (nothing launched) where it does not
+// apply or an allocation fails.
 template <int C, int P, bool WEIGHT>
 int scatter_interp(const ScatterArgs &a, dim3 grid, cudaStream_t stream) {
-    if constexpr (!(C == SO3G_COORD_CAR && (P == PX_FLAT_NT_NN || P == PX_HP_NT))) {
+    if constexpr (!(C == SO3G_COORD_CAR &&
+                    (P == PX_FLAT_NT_NN || P == PX_HP_NT || P == PX_HP_T))) {
         return 1;
     } else {
-        // Map offsets (key + plane offset) in 32 bits.
+        // Keys and plane offsets (key + plane offset untiled; within a tile
+        // tiled) in 32 bits.
         const long long nc = a.g.ncomp;
-        const long long npix = P == PX_HP_NT ? a.g.npix : (long long)a.g.ny * a.g.nx;
+        const long long npix = P == PX_FLAT_NT_NN ? (long long)a.g.ny * a.g.nx : a.g.npix;
         if (a.segs.seg || a.segs.n_time < 2 || nc < 1 || nc > 3 ||
             (WEIGHT ? nc * nc : nc) * npix >= (1LL << 31) || a.piece % kIxLen)
             return 1;
@@ -441,11 +472,11 @@ int scatter_interp(const ScatterArgs &a, dim3 grid, cudaStream_t stream) {
 // index does not fit 31 bits, or the mask cannot be allocated.
 template <int C, int P, bool WEIGHT>
 int scatter_mixed(const ScatterArgs &a, dim3 grid, cudaStream_t stream) {
+    const int ri = scatter_interp<C, P, WEIGHT>(a, grid, stream);
+    if (ri != 1) return ri;
     if constexpr (!MxEligible<C, P>::value) {
         return 1;
     } else {
-        const int ri = scatter_interp<C, P, WEIGHT>(a, grid, stream);
-        if (ri != 1) return ri;
         const long long npix = P == PX_HP_NT ? a.g.npix : (long long)a.g.ny * a.g.nx;
         if (!a.bore32 || npix >= (1LL << 31)) return 1;
         MxMask mm;

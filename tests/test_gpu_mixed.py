@@ -166,6 +166,61 @@ def test_mixed_to_map_layouts(pixelization, ncomp, accum):
     assert float(m.abs().sum()) > 0
 
 
+@pytest.mark.parametrize("accum", [_abi.ACCUM_WARP_RUNS, _abi.ACCUM_ATOMIC])
+def test_mixed_healpix_tiled_maps(accum):
+    """The chunked to_map / to_weight_map / from_map on a tiled NEST map
+    (nside 512, nside_tile 4: the run keys are parent NEST indices, each
+    run's tile looked up when it is flushed): unaligned signal rows, an odd
+    sample count, a scan across the belt / cap boundary, against the exact
+    path; a sample on an absent tile raises the tiling error in both
+    directions."""
+    import torch
+    from test_gpu_certified import _hp_engine
+    n_det, n_time = 24, 30_001
+    Q, dets, resp, gamma, sig = synth.workload(n_det, n_time, seed=63, radius_deg=3.0,
+                                               el=41.5, throw=40., v_az=2.)
+    p, eng = _hp_engine(512, True, True)
+    q = synth.native(p, Q)
+    qd, dd, rd = (torch.from_numpy(x).cuda() for x in (q, dets, resp))
+    wide = torch.zeros((n_det, n_time + 1), dtype=torch.float32, device="cuda")
+    wide[:, 1:] = torch.from_numpy(sig).cuda()
+    sv = wide[:, 1:]
+    nppt = eng._tile_pix_shape(0)[0]
+    n_tile = eng._n_tile()
+
+    def tiles(lead, skip=()):
+        return [None if i in skip else
+                torch.zeros(lead + (nppt,), dtype=torch.float64, device="cuda")
+                for i in range(n_tile)]
+
+    def flat(x):
+        return torch.cat([t.reshape(-1) for t in x]).double().cpu().numpy()
+
+    out = {}
+    for mode in MODES:
+        eng.pointing = mode
+        m = eng.to_map(tiles((3,)), qd, dd, rd, sv, None, None, accum=accum)
+        ww = eng.to_weight_map(tiles((3, 3)), qd, dd, rd, None, None, accum=accum)
+        base = torch.full((n_det, n_time + 1), 0.5, dtype=torch.float32, device="cuda")
+        src = out[_abi.POINTING_EXACT][0] if out else m
+        back = eng.from_map(src, qd, dd, rd, base[:, 1:])
+        out[mode] = [m, ww, back]
+    for a, b in zip(out[_abi.POINTING_EXACT], out[_abi.POINTING_MIXED]):
+        a = flat(a) if isinstance(a, list) else a.double().cpu().numpy()
+        b = flat(b) if isinstance(b, list) else b.double().cpu().numpy()
+        assert np.abs(a - b).max() <= 1e-6 * np.abs(a).max()
+    m_ex = out[_abi.POINTING_EXACT][0]
+    hit = [i for i, t in enumerate(m_ex) if float(t.abs().sum()) > 0]
+    assert 1 < len(hit) < n_tile
+    eng.pointing = _abi.POINTING_MIXED
+    gone = hit[len(hit) // 2]
+    with pytest.raises(RuntimeError, match=r"Tiling problem \(index %d\)" % gone):
+        eng.to_map(tiles((3,), skip=(gone,)), qd, dd, rd, sv, None, None, accum=accum)
+    src = [None if i == gone else t for i, t in enumerate(m_ex)]
+    with pytest.raises(RuntimeError, match=r"Tiling problem \(index %d\)" % gone):
+        eng.from_map(src, qd, dd, rd, None)
+
+
 def _probe_hp(eng, q, dets, resp, tiled, pf_bound=PF_BOUND_GUARD):
     import torch
     from test_gpu_certified import _hp_probe_maps
