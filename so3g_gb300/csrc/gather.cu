@@ -608,8 +608,14 @@ __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
                     // Tiled: the float32 copy spans the parent map, .w = 0
                     // on the pixels of absent tiles.
                     const float4 m = __ldg(a.map32 + key);
-                    if (P == PX_HP_T && m.w == 0.f) {
-                        record_missing_tile(a.err, key >> tsh);
+                    if ((P == PX_HP_T || P == PX_FLAT_T_NN) && m.w == 0.f) {
+                        if (P == PX_HP_T) {
+                            record_missing_tile(a.err, key >> tsh);
+                        } else {
+                            int tp[3];
+                            flat_tile_tuple(a.g, key / a.g.nx, key % a.g.nx, tp);
+                            record_missing_tile(a.err, tp[0]);
+                        }
                     } else {
                         // float32 terms (the mixed-precision contract).
                         float x = fmaf(m.x, pf[0], sv[i]);
@@ -654,20 +660,21 @@ __global__ void __launch_bounds__(kBlock) k_from_map_ix_fix(GatherArgs a, MxMask
                                   d2f_round(ofs.d)};
             float qb[4];
             load_bore_f32(a.bore32, a.bore, t, qb);
-            // Tiled HEALPix: the parent map's NEST index (the float32
-            // copy's index, .w = 0 on absent tiles).
+            // Tiled maps: the parent map's pixel (the float32 copy's
+            // index, .w = 0 on absent tiles).
+            constexpr bool kParent = P == PX_HP_T || P == PX_FLAT_T_NN;
             int pix[2];
             float pf[3] = {0.f, 0.f, 0.f};
             bool on = false;
-            if (!mixed_pointing<C, P, true, P == PX_HP_T>(a.g, a.ft, a.mc, qb, q32, nc, T, Pr,
-                                                          pix, on, pf))
+            if (!mixed_pointing<C, P, true, kParent>(a.g, a.ft, a.mc, qb, q32, nc, T, Pr, pix, on,
+                                                     pf))
                 return false;
             if (on) {
                 float *sp = a.signal + det * a.sig_stride + t;
-                const float4 m =
-                    __ldg(a.map32 + (P == PX_FLAT_NT_NN ? (long long)pix[0] * a.g.nx + pix[1]
-                                                        : (long long)pix[0]));
-                if (P == PX_HP_T && m.w == 0.f) {
+                const bool hp = P == PX_HP_NT || P == PX_HP_T;
+                const float4 m = __ldg(a.map32 + (hp ? (long long)pix[0]
+                                                     : (long long)pix[0] * a.g.nx + pix[1]));
+                if (kParent && m.w == 0.f) {
                     int tp[3];
                     parent_to_tile<P>(a.g, pix, tp);
                     record_missing_tile(a.err, tp[0]);
@@ -699,16 +706,17 @@ struct GatherIxFix {
     }
 };
 
-// The chunked from_map for CAR maps with the untiled nearest-neighbour
-// pixelizor and for HEALPix maps (untiled or tiled: the float32 copy spans
-// the parent map); returns 1 (nothing launched) where it does not apply.
+// The chunked from_map for CAR maps with the nearest-neighbour pixelizors
+// and for HEALPix maps (tiled maps: the float32 copy spans the parent map);
+// returns 1 (nothing launched) where it does not apply.
 template <int C, int P>
 int gather_interp(const GatherArgs &a, dim3 grid, cudaStream_t stream) {
-    if constexpr (!(C == SO3G_COORD_CAR &&
-                    (P == PX_FLAT_NT_NN || P == PX_HP_NT || P == PX_HP_T))) {
+    if constexpr (!(C == SO3G_COORD_CAR && (P == PX_FLAT_NT_NN || P == PX_FLAT_T_NN ||
+                                            P == PX_HP_NT || P == PX_HP_T))) {
         return 1;
     } else {
-        const long long npix = P == PX_FLAT_NT_NN ? (long long)a.g.ny * a.g.nx : a.g.npix;
+        const long long npix =
+            (P == PX_FLAT_NT_NN || P == PX_FLAT_T_NN) ? (long long)a.g.ny * a.g.nx : a.g.npix;
         if (a.segs.seg || a.segs.n_time < 2 || !a.map32 || npix >= (1LL << 31) ||
             a.g.ncomp < 1 || a.g.ncomp > 3 || a.piece % kIxLen)
             return 1;

@@ -430,8 +430,11 @@ __device__ __forceinline__ void ix_setup(const Args &a, const IxBore *ixb, int j
 // map (T; Q, U; or T, Q, U); false when its pixel is not certified.  The
 // fraction r of a pixel coordinate is certified when |r - 1/2| < 1/2 -
 // bound (r - 1/2 and 1/2 - bound are rounded by at most 2^-25, well inside
-// the bound's 1e-7 term).
-template <int NC>
+// the bound's 1e-7 term).  P = PX_FLAT_T_NN: the tiled pixelizor's rule
+// (int() truncation, src/Projection.cxx:1124-1138): on for coordinates in
+// (-1, n), those in (-1, 0) landing in row or column 0 -- a certified floor
+// of -1 lies strictly inside (-1, 0); key is the parent map's iy * nx + ix.
+template <int P, int NC>
 __device__ __forceinline__ bool ix_eval(const IxParams &p, float s, const DGeom &g, float T,
                                         float Pr, int &key, bool &on, float (&pf)[3]) {
     const float4 *w = reinterpret_cast<const float4 *>(&p);
@@ -440,8 +443,14 @@ __device__ __forceinline__ bool ix_eval(const IxParams &p, float s, const DGeom 
     const float y = fmaf(s, fmaf(s, fmaf(s, P1.w, P1.z), P1.y), P0.y);
     const float fxl = floorf(x), fyl = floorf(y);
     const bool ok = fabsf((x - fxl) - 0.5f) < P3.z && fabsf((y - fyl) - 0.5f) < P3.w;
-    const int ix = __float_as_int(P5.x) + (int)fxl, iy = __float_as_int(P5.y) + (int)fyl;
-    on = (unsigned)ix < (unsigned)g.nx && (unsigned)iy < (unsigned)g.ny;
+    int ix = __float_as_int(P5.x) + (int)fxl, iy = __float_as_int(P5.y) + (int)fyl;
+    if constexpr (P == PX_FLAT_T_NN) {
+        on = (unsigned)(ix + 1) < (unsigned)(g.nx + 1) && (unsigned)(iy + 1) < (unsigned)(g.ny + 1);
+        ix = max(ix, 0);
+        iy = max(iy, 0);
+    } else {
+        on = (unsigned)ix < (unsigned)g.nx && (unsigned)iy < (unsigned)g.ny;
+    }
     key = iy * g.nx + ix;
     if constexpr (NC == 1) {
         pf[0] = T;
@@ -501,9 +510,9 @@ __device__ __forceinline__ bool ix_eval_hp(const IxParams &pr, float s, const DG
     return ok;
 }
 
-// One sample of the chunked pointing for pixelizor P (CAR untiled nearest
-// or HEALPix): ok (certified), key (map index; tiled HEALPix: the parent
-// map's NEST index), on, spin factors.
+// One sample of the chunked pointing for pixelizor P (CAR nearest or
+// HEALPix): ok (certified), key (map index; tiled maps: the parent map's
+// index), on, spin factors.
 template <int P, int NC>
 __device__ __forceinline__ bool ix_sample(const IxParams &p, float s, const DGeom &g, float T,
                                           float Pr, int &key, bool &on, float (&pf)[3]) {
@@ -511,7 +520,7 @@ __device__ __forceinline__ bool ix_sample(const IxParams &p, float s, const DGeo
         on = true;
         return ix_eval_hp<P, NC>(p, s, g, T, Pr, key, pf);
     } else {
-        return ix_eval<NC>(p, s, g, T, Pr, key, on, pf);
+        return ix_eval<P, NC>(p, s, g, T, Pr, key, on, pf);
     }
 }
 

@@ -198,6 +198,7 @@ struct IxValues {
 // untiled map; on a tiled HEALPix map (key = the parent NEST index) the
 // element of its tile (tile = key >> tsh, tsh = log2 of the pixels per
 // tile), NULL with the missing-tile error recorded when the tile is absent.
+// (Tiled flat maps: ix_flush_run.)
 template <int P>
 __device__ __forceinline__ double *ix_base(const ScatterArgs &a, int key, int tsh) {
     if (key < 0) return nullptr;
@@ -215,14 +216,35 @@ __device__ __forceinline__ double *ix_base(const ScatterArgs &a, int key, int ts
 }
 
 // One run total of k_scatter_ix4 added to the map (key < 0: nothing); off
-// holds the values' plane offsets within the map (or the tile).
-template <int P, int NV>
-__device__ __forceinline__ void ix_flush_run(const ScatterArgs &a, int key, int tsh,
+// holds the values' plane offsets within the map (or the HEALPix tile).  A
+// tiled flat map's key (the parent map's iy * nx + ix) is split into its
+// tile tuple when the run is flushed, the tile's own plane size (edge
+// tiles are smaller) giving the offsets.  aux: log2 of the pixels per tile
+// (tiled HEALPix), the bits of 1/nx as a float (tiled flat).
+template <int P, bool WEIGHT, int NC, int NV>
+__device__ __forceinline__ void ix_flush_run(const ScatterArgs &a, int key, int aux,
                                              const int (&off)[NV], const float (&v)[NV]) {
-    double *p = ix_base<P>(a, key, tsh);
-    if (p) {
+    if constexpr (P == PX_FLAT_T_NN) {
+        if (key < 0) return;
+        const int iy = div_small(key, a.g.nx, __int_as_float(aux)), ix = key - iy * a.g.nx;
+        int tp[3];
+        flat_tile_tuple(a.g, iy, ix, tp);
+        long long o, plane;
+        const int bad = locate<P>(a.g, tp, &o, &plane);
+        if (bad >= 0) {
+            record_missing_tile(a.err, bad);
+            return;
+        }
+        int po[NV];
+        IxValues<WEIGHT, NC>::offsets((int)plane, po);
 #pragma unroll
-        for (int k = 0; k < NV; k++) atomicAdd(p + off[k], f2d(v[k]));
+        for (int k = 0; k < NV; k++) atomicAdd(a.map + o + po[k], f2d(v[k]));
+    } else {
+        double *p = ix_base<P>(a, key, aux);
+        if (p) {
+#pragma unroll
+            for (int k = 0; k < NV; k++) atomicAdd(p + off[k], f2d(v[k]));
+        }
     }
 }
 
@@ -259,7 +281,8 @@ __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
     int off[NV];
     V::offsets(P == PX_HP_NT ? (int)a.g.npix : (P == PX_HP_T ? (int)a.g.nppt : a.g.ny * a.g.nx),
                off);
-    const int tsh = P == PX_HP_T ? __ffsll(a.g.nppt) - 1 : 0;
+    const int aux = P == PX_HP_T ? __ffsll(a.g.nppt) - 1
+                    : (P == PX_FLAT_T_NN ? __float_as_int(1.f / (float)a.g.nx) : 0);
     const float *sig = WEIGHT ? nullptr : a.signal + det * a.sig_stride;
     const bool vec = (reinterpret_cast<unsigned long long>(sig) & 15) == 0;
     unsigned *mwb = mm.words + ((long long)blockIdx.x * gridDim.y + blockIdx.y) * mm.wpp;
@@ -322,7 +345,8 @@ __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
             }
             if (a.accum != SO3G_ACCUM_WARP_RUNS) {
 #pragma unroll
-                for (int i = 0; i < 4; i++) ix_flush_run<P, NV>(a, key[i], tsh, off, v[i]);
+                for (int i = 0; i < 4; i++)
+                    ix_flush_run<P, WEIGHT, NC, NV>(a, key[i], aux, off, v[i]);
                 continue;
             }
             // Run heads and right-to-left run totals (in place: v[i] becomes
@@ -346,11 +370,13 @@ __global__ void __launch_bounds__(kBlock, kIxBlocksPerSM)
             }
             ks1 = h1 ? key[1] : (h2 ? key[2] : key[3]);
             ks2 = (h1 && h2) ? key[2] : key[3];
-            ix_flush_run<P, NV>(a, key[0], tsh, off, v[0]);
-            if (__any_sync(kFull, nruns > 1) && nruns > 1) ix_flush_run<P, NV>(a, ks1, tsh, off, s1);
-            if (__any_sync(kFull, nruns > 2) && nruns > 2) ix_flush_run<P, NV>(a, ks2, tsh, off, s2);
+            ix_flush_run<P, WEIGHT, NC, NV>(a, key[0], aux, off, v[0]);
+            if (__any_sync(kFull, nruns > 1) && nruns > 1)
+                ix_flush_run<P, WEIGHT, NC, NV>(a, ks1, aux, off, s1);
+            if (__any_sync(kFull, nruns > 2) && nruns > 2)
+                ix_flush_run<P, WEIGHT, NC, NV>(a, ks2, aux, off, s2);
             if (__any_sync(kFull, nruns > 3) && nruns > 3)
-                ix_flush_run<P, NV>(a, key[3], tsh, off, v[3]);
+                ix_flush_run<P, WEIGHT, NC, NV>(a, key[3], aux, off, v[3]);
         }
         __syncwarp();
     }
@@ -375,7 +401,7 @@ __global__ void __launch_bounds__(kBlock) k_scatter_ix_fix(ScatterArgs a, MxMask
                                   d2f_round(ofs.d)};
             float qb[4];
             load_bore_f32(a.bore32, a.bore, t, qb);
-            int pix[2];
+            int pix[3];   // a tiled flat map's tuple: tile, row, column
             float pf[3] = {0.f, 0.f, 0.f};
             bool on = false;
             if (!mixed_pointing<C, P, true, false>(a.g, a.ft, a.mc, qb, q32, nc, T, Pr, pix, on,
@@ -426,20 +452,21 @@ struct ScatterMxFix {
     }
 };
 
-// The chunked pointing for CAR maps with the untiled nearest-neighbour
-// pixelizor and for HEALPix maps (untiled or tiled), over whole detectors
+// The chunked pointing for CAR maps with the nearest-neighbour pixelizors
+// and for HEALPix maps (untiled or tiled), over whole detectors
 // (no sample segments); returns 1 (nothing launched) where it does not
 // apply or an allocation fails.
 template <int C, int P, bool WEIGHT>
 int scatter_interp(const ScatterArgs &a, dim3 grid, cudaStream_t stream) {
-    if constexpr (!(C == SO3G_COORD_CAR &&
-                    (P == PX_FLAT_NT_NN || P == PX_HP_NT || P == PX_HP_T))) {
+    if constexpr (!(C == SO3G_COORD_CAR && (P == PX_FLAT_NT_NN || P == PX_FLAT_T_NN ||
+                                            P == PX_HP_NT || P == PX_HP_T))) {
         return 1;
     } else {
         // Keys and plane offsets (key + plane offset untiled; within a tile
         // tiled) in 32 bits.
         const long long nc = a.g.ncomp;
-        const long long npix = P == PX_FLAT_NT_NN ? (long long)a.g.ny * a.g.nx : a.g.npix;
+        const long long npix =
+            (P == PX_FLAT_NT_NN || P == PX_FLAT_T_NN) ? (long long)a.g.ny * a.g.nx : a.g.npix;
         if (a.segs.seg || a.segs.n_time < 2 || nc < 1 || nc > 3 ||
             (WEIGHT ? nc * nc : nc) * npix >= (1LL << 31) || a.piece % kIxLen)
             return 1;
