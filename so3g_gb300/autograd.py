@@ -9,8 +9,9 @@ to_map applied to the incoming signal gradient, so that
 
 and gradients of any loss of the projected signal flow back to the map.
 Both directions run the CUDA kernels of this package on the current
-stream.  Maps are untiled CUDA float64 tensors of shape (n_comp, ...); the
-signal is float32 (n_det, n_time).  The engine's pointing mode is read once,
+stream.  Maps are CUDA float64 tensors of shape (n_comp, ...), or for a
+tiled engine lists of such tiles (None for an absent tile; a gradient is
+returned for each present one); the signal is float32 (n_det, n_time).  The engine's pointing mode is read once,
 in forward, and backward runs to_map in that same mode, so that the pair
 stays an adjoint pair even if the caller changes ``eng.pointing`` between
 the two.
@@ -46,7 +47,7 @@ class FromMap(torch.autograd.Function):
         if not (isinstance(map, torch.Tensor) and map.is_cuda and map.dtype == torch.float64):
             raise TypeError("FromMap needs a CUDA float64 map tensor")
         if getattr(eng, "_tiled", False):
-            raise TypeError("FromMap supports untiled maps only")
+            raise TypeError("FromMap takes untiled maps; tiled maps go through FromMapTiled")
         ctx.eng = eng
         ctx.mode = getattr(eng, "pointing", DEFAULT_POINTING)
         ctx.save_for_backward(boresight, dets, response)
@@ -65,8 +66,51 @@ class FromMap(torch.autograd.Function):
         return gmap, None, None, None, None
 
 
+class FromMapTiled(torch.autograd.Function):
+    """FromMap for a tiled engine: the present tiles are the function's
+    tensor inputs (autograd tracks only direct tensor arguments), `present`
+    their tile numbers; backward returns to_map's tiles as their
+    gradients."""
+
+    @staticmethod
+    def forward(ctx, eng, boresight, dets, response, present, n_tile, *tiles):
+        for t in tiles:
+            if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float64):
+                raise TypeError("FromMap needs CUDA float64 tile tensors")
+        ctx.eng = eng
+        ctx.mode = getattr(eng, "pointing", DEFAULT_POINTING)
+        ctx.present = present
+        ctx.n_tile = n_tile
+        ctx.shapes = [tuple(t.shape) for t in tiles]
+        ctx.save_for_backward(boresight, dets, response)
+        full = [None] * n_tile
+        for i, t in zip(present, tiles):
+            full[i] = t.detach().contiguous()
+        with torch.no_grad():
+            sig = eng.from_map(full, boresight, dets, response, None)
+        return sig
+
+    @staticmethod
+    def backward(ctx, grad_sig):
+        boresight, dets, response = ctx.saved_tensors
+        g = grad_sig.detach().to(torch.float32).contiguous()
+        grads = [torch.zeros(sh, dtype=torch.float64, device=g.device) for sh in ctx.shapes]
+        full = [None] * ctx.n_tile
+        for i, t in zip(ctx.present, grads):
+            full[i] = t
+        with _pointing(ctx.eng, ctx.mode):
+            ctx.eng.to_map(full, boresight, dets, response, g, None, None)
+        return (None, None, None, None, None, None) + tuple(grads)
+
+
 def from_map(eng, map, boresight, dets, response):
     """Differentiable ``eng.from_map(map, boresight, dets, response)``: the
     inputs other than the map are CUDA tensors (boresight (n_time, 4) and
-    dets (n_det, 4) float64, response (n_det, 2) float32)."""
+    dets (n_det, 4) float64, response (n_det, 2) float32).  A tiled
+    engine's map is a list of tiles (None: absent); its present tiles get
+    gradients."""
+    if isinstance(map, (list, tuple)):
+        present = tuple(i for i, t in enumerate(map) if t is not None)
+        return FromMapTiled.apply(eng, boresight, dets, response, present, len(map),
+                                  *[map[i] for i in present])
     return FromMap.apply(map, eng, boresight, dets, response)

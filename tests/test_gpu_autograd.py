@@ -108,3 +108,50 @@ def test_backward_uses_the_forward_pointing_mode():
     # The two modes' maps differ (float32 spin factors), so the check above
     # does tell them apart.
     assert float((exact - want).abs().max()) > 1e-12 * scale
+
+
+def _setup_tiled(n_det=16, n_time=20000, shape=(200, 240)):
+    import torch
+    Q, dets, resp, gamma, _ = synth.workload(n_det, n_time, seed=23, radius_deg=0.5,
+                                             throw=2.)
+    ny, nx = shape
+    r = 2 * ARCMIN * 180 / np.pi
+    w = SimpleWCS("CAR", (-180., 50.), (-r, r), (nx / 2 + 0.5, ny / 2 + 0.5))
+    p = Projectionist.for_tiled((ny, nx), w, (64, 96))
+    q = synth.native(p, Q)
+    eng = p.get_ProjEng("TQU")
+    t = [torch.from_numpy(x).cuda() for x in (q, dets, resp)]
+    rng = np.random.default_rng(6)
+    tiles = [torch.from_numpy(rng.standard_normal((3,) + tuple(eng._tile_pix_shape(i)))).cuda()
+             for i in range(eng._n_tile())]
+    d = torch.from_numpy(rng.standard_normal((n_det, n_time)).astype(np.float32)).cuda()
+    return eng, t, tiles, d
+
+
+def test_tiled_backward_is_to_map_and_adjoint():
+    """A tiled map (a list of tiles, one absent and never hit): the
+    gradient of each present tile is to_map's tile, <P m, d> = <m, P^T d>,
+    and the absent tile gets no gradient."""
+    import torch
+    eng, (q, dets, resp), tiles, d = _setup_tiled()
+    hits = eng.to_map([torch.zeros_like(t) for t in tiles], q, dets, resp,
+                      torch.ones_like(d), None, None)
+    cold = [i for i, t in enumerate(hits) if float(t.abs().sum()) == 0]
+    assert cold
+    tiles[cold[0]] = None
+    leaves = [None if t is None else t.clone().requires_grad_(True) for t in tiles]
+    sig = autograd.from_map(eng, leaves, q, dets, resp)
+    (sig * d).sum().backward()
+    want = eng.to_map([None if t is None else torch.zeros_like(t) for t in tiles], q, dets,
+                      resp, d, None, None)
+    lhs = float((sig.detach().double() * d.double()).sum())
+    rhs = 0.
+    for leaf, w in zip(leaves, want):
+        if leaf is None:
+            assert w is None
+            continue
+        assert torch.allclose(leaf.grad, w, rtol=1e-12, atol=1e-12 * float(w.abs().max()) + 1e-300)
+        rhs += float((leaf.detach() * w).sum())
+    scale = float((sig.detach().double().abs() * d.double().abs()).sum())
+    assert abs(lhs - rhs) <= 1e-6 * scale
+
