@@ -111,6 +111,8 @@ def test_backward_uses_the_forward_pointing_mode():
 
 
 def _setup_tiled(n_det=16, n_time=20000, shape=(200, 240)):
+    """A tiled CAR engine whose active tiles are the ones the scan hits
+    (the others absent), its inputs, random tiles and a signal."""
     import torch
     Q, dets, resp, gamma, _ = synth.workload(n_det, n_time, seed=23, radius_deg=0.5,
                                              throw=2.)
@@ -122,23 +124,25 @@ def _setup_tiled(n_det=16, n_time=20000, shape=(200, 240)):
     eng = p.get_ProjEng("TQU")
     t = [torch.from_numpy(x).cuda() for x in (q, dets, resp)]
     rng = np.random.default_rng(6)
-    tiles = [torch.from_numpy(rng.standard_normal((3,) + tuple(eng._tile_pix_shape(i)))).cuda()
-             for i in range(eng._n_tile())]
     d = torch.from_numpy(rng.standard_normal((n_det, n_time)).astype(np.float32)).cuda()
+    shapes = [(3,) + tuple(eng._tile_pix_shape(i)) for i in range(eng._n_tile())]
+    hits = eng.to_map([torch.zeros(sh, dtype=torch.float64, device="cuda") for sh in shapes],
+                      t[0], t[1], t[2], torch.ones_like(d), None, None)
+    active = [i for i, h in enumerate(hits) if float(h.abs().sum()) > 0]
+    assert 0 < len(active) < len(shapes)
+    p = Projectionist.for_tiled((ny, nx), w, (64, 96), active_tiles=active)
+    eng = p.get_ProjEng("TQU")
+    tiles = [torch.from_numpy(rng.standard_normal(sh)).cuda() if i in active else None
+             for i, sh in enumerate(shapes)]
     return eng, t, tiles, d
 
 
 def test_tiled_backward_is_to_map_and_adjoint():
-    """A tiled map (a list of tiles, one absent and never hit): the
+    """A tiled map (a list of tiles, those the scan never hits absent): the
     gradient of each present tile is to_map's tile, <P m, d> = <m, P^T d>,
-    and the absent tile gets no gradient."""
+    and the absent tiles get no gradient."""
     import torch
     eng, (q, dets, resp), tiles, d = _setup_tiled()
-    hits = eng.to_map([torch.zeros_like(t) for t in tiles], q, dets, resp,
-                      torch.ones_like(d), None, None)
-    cold = [i for i, t in enumerate(hits) if float(t.abs().sum()) == 0]
-    assert cold
-    tiles[cold[0]] = None
     leaves = [None if t is None else t.clone().requires_grad_(True) for t in tiles]
     sig = autograd.from_map(eng, leaves, q, dets, resp)
     (sig * d).sum().backward()
@@ -150,8 +154,8 @@ def test_tiled_backward_is_to_map_and_adjoint():
         if leaf is None:
             assert w is None
             continue
-        assert torch.allclose(leaf.grad, w, rtol=1e-12, atol=1e-12 * float(w.abs().max()) + 1e-300)
+        assert torch.allclose(leaf.grad, w, rtol=1e-12,
+                              atol=1e-12 * float(w.abs().max()) + 1e-300)
         rhs += float((leaf.detach() * w).sum())
     scale = float((sig.detach().double().abs() * d.double().abs()).sum())
     assert abs(lhs - rhs) <= 1e-6 * scale
-
