@@ -1126,7 +1126,7 @@ def _edges_to_ranges(e, n_det, n_time, n_domain):
             for a, b in zip(starts.tolist(), stops.tolist()):
                 d, k = divmod(int(key[a]), n_det)
                 target = par[d] if d < n_domain else ser[0]
-                target[k]._segs = pairs[a:b].tolist()
+                target[k]._set(pairs[a:b])
         finally:
             if was_enabled:
                 gc.enable()

@@ -8,26 +8,57 @@ which does not.  RangesMatrix follows python/proj/ranges.py:11-297: a
 nested container of Ranges whose last axis is the sample axis.
 
 These are host-side containers (the argument type of ``thread_intervals``),
-kept in numpy; the projection kernels receive them flattened to
+kept in numpy arrays; the projection kernels receive them flattened to
 (det, start, end) segments.
 """
 import numpy as np
 
 
+_NO_SEGS = np.zeros((0, 2), dtype=np.int64)
+
+
 class RangesInt32:
-    """Half-open intervals over ``count`` samples."""
+    """Half-open intervals over ``count`` samples.
+
+    The intervals live in an (n, 2) int64 numpy array; intervals added one
+    at a time (append_interval_no_check, as the thread assignment loops do)
+    collect in a short Python list that is folded into the array when the
+    intervals are next read, so neither appending nor reading costs a
+    Python object per interval."""
 
     def __init__(self, count=0, reference=0):
         self.count = int(count)
         self.reference = int(reference)
-        self._segs = []  # list of [start, end]
+        self._a = _NO_SEGS
+        self._tail = []   # [start, end] pairs appended since the last fold
+
+    def _arr(self):
+        """The intervals as an (n, 2) int64 array, in storage order."""
+        if self._tail:
+            t = np.asarray(self._tail, dtype=np.int64).reshape(-1, 2)
+            self._a = np.concatenate([self._a, t]) if len(self._a) else t
+            self._tail = []
+        return self._a
+
+    def _set(self, pairs):
+        self._a = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
+        self._tail = []
+
+    @property
+    def _segs(self):
+        """The intervals as a list of [start, end] lists."""
+        return self._arr().tolist()
+
+    @_segs.setter
+    def _segs(self, pairs):
+        self._set(pairs)
 
     # -- construction --------------------------------------------------------
     @classmethod
     def from_array(cls, intervals, count):
         r = cls(count)
-        for a, b in np.asarray(intervals, dtype=np.int64).reshape(-1, 2):
-            r.add_interval(int(a), int(b))
+        r._set(intervals)
+        r._cleanup()
         return r
 
     @classmethod
@@ -37,15 +68,13 @@ class RangesInt32:
             return RangesMatrix([cls.from_mask(m) for m in mask])
         r = cls(len(mask))
         if len(mask):
-            d = np.diff(np.concatenate([[0], mask.astype(np.int8), [0]]))
-            starts = np.nonzero(d == 1)[0]
-            ends = np.nonzero(d == -1)[0]
-            r._segs = [[int(a), int(b)] for a, b in zip(starts, ends)]
+            d = np.diff(mask.astype(np.int8), prepend=np.int8(0), append=np.int8(0))
+            r._set(np.stack([np.flatnonzero(d == 1), np.flatnonzero(d == -1)], axis=1))
         return r
 
     def copy(self):
         r = RangesInt32(self.count, self.reference)
-        r._segs = [list(s) for s in self._segs]
+        r._a = self._arr().copy()
         return r
 
     def zeros_like(self):
@@ -54,54 +83,73 @@ class RangesInt32:
     def ones_like(self):
         r = RangesInt32(self.count, self.reference)
         if self.count > 0:
-            r._segs = [[0, self.count]]
+            r._set([[0, self.count]])
         return r
 
     # -- basic operations ------------------------------------------------------
     def append_interval_no_check(self, start, end):
-        self._segs.append([int(start), int(end)])
+        self._tail.append([int(start), int(end)])
         return self
 
     def add_interval(self, start, end):
-        start, end = int(start), int(end)
-        self._segs.append([start, end])
+        self._tail.append([int(start), int(end)])
         self._cleanup()
         return self
 
     def _cleanup(self):
-        segs = sorted((max(0, a), min(self.count, b)) for a, b in self._segs)
-        out = []
-        for a, b in segs:
-            if b <= a:
-                continue
-            if out and a <= out[-1][1]:
-                out[-1][1] = max(out[-1][1], b)
-            else:
-                out.append([a, b])
-        self._segs = out
+        """Clips to [0, count), drops empty intervals, sorts and merges the
+        overlapping or touching ones."""
+        a = self._arr()
+        if not len(a):
+            return
+        lo = np.maximum(a[:, 0], 0)
+        hi = np.minimum(a[:, 1], self.count)
+        keep = hi > lo
+        lo, hi = lo[keep], hi[keep]
+        if not len(lo):
+            self._a = _NO_SEGS
+            return
+        o = np.lexsort((hi, lo))
+        lo, hi = lo[o], hi[o]
+        # An interval opens a new run when it starts past every earlier end.
+        new = np.empty(len(lo), dtype=bool)
+        new[0] = True
+        new[1:] = lo[1:] > np.maximum.accumulate(hi)[:-1]
+        first = np.flatnonzero(new)
+        self._a = np.stack([lo[first], np.maximum.reduceat(hi, first)], axis=1)
 
     def merge(self, src):
-        self._segs.extend(list(s) for s in src._segs)
+        a = src._arr()
+        if len(a):
+            self._tail.extend(a.tolist())
         self._cleanup()
         return self
 
     def intersect(self, src):
-        self._segs = (self * src)._segs
+        self._set((self * src)._arr())
         return self
 
     def complement(self):
         out = RangesInt32(self.count, self.reference)
-        x = 0
-        for a, b in sorted(self._segs):
-            if a > x:
-                out._segs.append([x, a])
-            x = max(x, b)
-        if x < self.count:
-            out._segs.append([x, self.count])
+        a = self._arr()
+        if not len(a):
+            if self.count > 0:
+                out._set([[0, self.count]])
+            return out
+        o = np.lexsort((a[:, 1], a[:, 0]))
+        lo, hi = a[o, 0], a[o, 1]
+        # x before interval i: the largest end so far (0 at the start).
+        x = np.maximum.accumulate(np.concatenate([[0], hi]))
+        gap = lo > x[:-1]
+        pairs = np.stack([x[:-1][gap], lo[gap]], axis=1)
+        if x[-1] < self.count:
+            pairs = np.concatenate([pairs, [[x[-1], self.count]]])
+        out._set(pairs)
         return out
 
     def buffer(self, buff):
-        self._segs = [[a - buff, b + buff] for a, b in self._segs]
+        a = self._arr()
+        self._set(a + np.array([-int(buff), int(buff)], dtype=np.int64))
         self._cleanup()
         return self
 
@@ -116,21 +164,24 @@ class RangesInt32:
                 out[-1][1] = max(out[-1][1], b)
             else:
                 out.append([a, b])
-        self._segs = out
+        self._set(out)
         return self
 
     # -- views -----------------------------------------------------------------
     def ranges(self):
         """(n, 2) int32 array of [start, end) pairs."""
-        if not self._segs:
-            return np.zeros((0, 2), dtype=np.int32)
-        return np.array(self._segs, dtype=np.int32).reshape(-1, 2)
+        return self._arr().astype(np.int32)
 
     def mask(self):
-        m = np.zeros(self.count, dtype=bool)
-        for a, b in self._segs:
-            m[max(a, 0):max(b, 0)] = True
-        return m
+        m = np.zeros(self.count + 1, dtype=np.int32)
+        a = self._arr()
+        if len(a):
+            lo = np.clip(a[:, 0], 0, self.count)
+            hi = np.clip(a[:, 1], 0, self.count)
+            keep = hi > lo
+            np.add.at(m, lo[keep], 1)
+            np.add.at(m, hi[keep], -1)
+        return np.cumsum(m[:-1]) > 0
 
     @property
     def shape(self):
@@ -149,7 +200,7 @@ class RangesInt32:
         return self.copy().merge(other)
 
     def __mul__(self, other):
-        out = RangesInt32(self.count, self.reference)
+        out = []
         a = sorted(self._segs)
         b = sorted(other._segs)
         i = j = 0
@@ -157,12 +208,14 @@ class RangesInt32:
             lo = max(a[i][0], b[j][0])
             hi = min(a[i][1], b[j][1])
             if hi > lo:
-                out._segs.append([lo, hi])
+                out.append([lo, hi])
             if a[i][1] < b[j][1]:
                 i += 1
             else:
                 j += 1
-        return out
+        r = RangesInt32(self.count, self.reference)
+        r._set(out)
+        return r
 
     def __getitem__(self, index):
         if not isinstance(index, slice):
@@ -171,14 +224,16 @@ class RangesInt32:
         if step != 1:
             raise IndexError("RangesInt32 slices must have unit step")
         out = RangesInt32(max(0, stop - start), self.reference + start)
-        for a, b in self._segs:
-            lo, hi = max(a, start) - start, min(b, stop) - start
-            if hi > lo:
-                out._segs.append([lo, hi])
+        a = self._arr()
+        if len(a):
+            lo = np.maximum(a[:, 0], start) - start
+            hi = np.minimum(a[:, 1], stop) - start
+            keep = hi > lo
+            out._set(np.stack([lo[keep], hi[keep]], axis=1))
         return out
 
     def __repr__(self):
-        return "RangesInt32(n=%d:rngs=%d)" % (self.count, len(self._segs))
+        return "RangesInt32(n=%d:rngs=%d)" % (self.count, len(self._arr()))
 
 
 class RangesMatrix:
