@@ -18,9 +18,9 @@ ARCMIN = np.pi / 180 / 60
 MODES = (_abi.POINTING_EXACT, _abi.POINTING_CERTIFIED, _abi.POINTING_MIXED)
 
 
-def _case(seed):
+def _case(seed, kinds=("CAR", "TAN", "ZEA", "SIN", "HP", "ARC")):
     rng = np.random.default_rng(1000 + seed)
-    kind = ["CAR", "TAN", "ZEA", "SIN", "HP", "ARC"][seed % 6]
+    kind = kinds[seed % len(kinds)]
     el = float(rng.uniform(20., 75.))
     az0 = float(rng.uniform(0., 360.))
     n_det = 8
@@ -35,6 +35,8 @@ def _case(seed):
         nside = int(rng.choice([64, 256, 1024]))
         nest = bool(rng.integers(0, 2))
         tiled = nest and bool(rng.integers(0, 2))
+        if len(kinds) == 2 and nest:   # the chunked sweep tiles every NEST map
+            tiled = True
         p, eng = _hp_engine(nside, nest, tiled)
         maps = _hp_probe_maps(eng, tiled, 3)
     else:
@@ -54,8 +56,19 @@ def _case(seed):
 
 @pytest.mark.parametrize("seed", range(36))
 def test_random_geometry(gpulib, seed):
+    _check_geometry(_case(seed))
+
+
+@pytest.mark.parametrize("seed", range(100, 124))
+def test_random_geometry_chunked(gpulib, seed):
+    """The same sweep over the geometries the chunked mixed kernels take
+    (CAR and HEALPix, untiled and tiled, ragged edge tiles)."""
+    _check_geometry(_case(seed, kinds=("CAR", "HP")))
+
+
+def _check_geometry(case):
     import torch
-    kind, eng, maps, q, dets, resp = _case(seed)
+    kind, eng, maps, q, dets, resp = case
     qd, dd, rd = (torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in (q, dets, resp))
     out = {}
     for mode in MODES:
