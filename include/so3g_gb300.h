@@ -196,6 +196,15 @@ int so3g_get_trig_tables(double *asin_vals, double *atan2_vals, int32_t n);
 /* Number of kernel launches this library has enqueued since load. */
 int64_t so3g_launch_count(void);
 
+/* Sets the smallest call (detectors x samples of a call over whole
+ * detectors) that takes the chunked mixed-pointing kernels, and returns
+ * the previous value (default 30,000,000; no counterpart in the reference,
+ * whose pointing has one form).  Smaller calls take the per-sample float32
+ * tier, whose fixed cost per call is lower; results agree within the mixed
+ * pointing's tolerance either way.  Process-wide; negative values count as
+ * 0 (every eligible call chunked). */
+int64_t so3g_set_chunked_min_samples(int64_t n);
+
 /* How the current device can reach host memory at `ptr` (no counterpart
  * in the reference, whose arrays are all host memory).  Sets *mode to
  *   SO3G_HOST_NONE     not reachable: copy it to the device first;

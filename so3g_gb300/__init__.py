@@ -32,6 +32,15 @@ def version():
     return __version__
 
 
+def set_chunked_min_samples(n):
+    """Sets the smallest call (detectors x samples, whole detectors) that
+    takes the chunked mixed-pointing kernels; returns the previous value
+    (default 3e7: smaller calls take the per-sample float32 tier, whose
+    fixed cost per call is lower).  Process-wide."""
+    from . import _abi
+    return int(_abi.lib().so3g_set_chunked_min_samples(int(n)))
+
+
 def useful_info():
     """so3g's useful_info() (src/main.cxx:26-39).  omp_num_threads is the
     host thread count used by the thread-assignment helpers."""

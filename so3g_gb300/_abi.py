@@ -110,6 +110,7 @@ _SIGS = {
     "so3g_abi_version": (ctypes.c_int, []),
     "so3g_get_trig_tables": (ctypes.c_int, [c_void_p, c_void_p, c_int32]),
     "so3g_launch_count": (c_int64, []),
+    "so3g_set_chunked_min_samples": (c_int64, [c_int64]),
     "so3g_host_access": (ctypes.c_int, [c_void_p, c_void_p]),
     "so3g_proj_coords": (ctypes.c_int, [P(Pixelization), c_void_p, c_int32, c_void_p, c_int32,
                                         c_void_p, c_void_p]),

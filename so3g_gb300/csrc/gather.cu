@@ -718,7 +718,8 @@ int gather_interp(const GatherArgs &a, dim3 grid, cudaStream_t stream) {
         const long long npix =
             (P == PX_FLAT_NT_NN || P == PX_FLAT_T_NN) ? (long long)a.g.ny * a.g.nx : a.g.npix;
         if (a.segs.seg || a.segs.n_time < 2 || !a.map32 || npix >= (1LL << 31) ||
-            a.g.ncomp < 1 || a.g.ncomp > 3 || a.piece % kIxLen)
+            a.g.ncomp < 1 || a.g.ncomp > 3 || a.piece % kIxLen ||
+            (long long)grid.x * a.segs.n_time < chunked_min_samples())
             return 1;
         IxBore *ixb = ix_bore_models(a.bore, a.segs.n_time, stream);
         if (!ixb) return 1;

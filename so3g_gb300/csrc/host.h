@@ -15,6 +15,10 @@ int set_error(int code, const char *fmt, ...);
 void clear_error();
 // Checks cudaGetLastError() after a launch; counts the launch.
 int after_launch(const char *what);
+// Smallest call (detectors x samples) that takes the chunked mixed kernels
+// (so3g_set_chunked_min_samples); smaller calls take the per-sample float32
+// tier, whose fixed cost per call is lower.
+long long chunked_min_samples();
 // Per-device trig table (asin then atan2, 2 x kLutN float64), or NULL.
 const double *device_lut();
 

@@ -33,6 +33,21 @@ def pytest_collection_modifyitems(config, items):
             item.add_marker(skip)
 
 
+@pytest.fixture(autouse=True)
+def _chunked_at_every_size(request):
+    """GPU tests take the chunked mixed kernels at every call size (the
+    library takes them from ~3e7 samples per call on), so that their small
+    cases exercise them; a test of the per-sample tier raises the threshold
+    itself (it is restored after every test)."""
+    if request.node.get_closest_marker("gpu") is None or not HAS_GPU:
+        yield
+        return
+    from so3g_gb300 import set_chunked_min_samples
+    old = set_chunked_min_samples(0)
+    yield
+    set_chunked_min_samples(old)
+
+
 @pytest.fixture(scope="session")
 def orc():
     from oracle import Oracle

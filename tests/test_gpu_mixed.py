@@ -120,15 +120,20 @@ def test_mixed_maps_within_tolerance(tiled):
 @pytest.mark.parametrize("pixelization", ["car", "hp_ring", "hp_nest"])
 @pytest.mark.parametrize("ncomp", [1, 2, 3])
 @pytest.mark.parametrize("accum", [_abi.ACCUM_WARP_RUNS, _abi.ACCUM_ATOMIC])
-def test_mixed_to_map_layouts(pixelization, ncomp, accum):
-    """The chunked to_map / to_weight_map / from_map (CAR untiled nearest,
-    HEALPix untiled) with signal rows that are not 16-byte aligned (a
-    column slice of a wider array), an odd sample count (a partial last
-    chunk and an odd chunk count per piece), detector weights with zeros,
-    every component count and both accumulation modes, against the exact
-    path.  The HEALPix scan crosses the belt / cap boundary (|z| = 2/3)."""
+@pytest.mark.parametrize("path", ["chunked", "per_sample"])
+def test_mixed_to_map_layouts(pixelization, ncomp, accum, path):
+    """The mixed to_map / to_weight_map / from_map (CAR untiled nearest,
+    HEALPix untiled), through the chunked kernels and through the
+    per-sample tier that calls below the chunked threshold take, with
+    signal rows that are not 16-byte aligned (a column slice of a wider
+    array), an odd sample count (a partial last chunk and an odd chunk
+    count per piece), detector weights with zeros, every component count
+    and both accumulation modes, against the exact path.  The HEALPix scan
+    crosses the belt / cap boundary (|z| = 2/3)."""
     import torch
+    import so3g_gb300
     from test_gpu_certified import _hp_engine
+    so3g_gb300.set_chunked_min_samples(0 if path == "chunked" else 1 << 62)
     n_det, n_time = 24, 30_001
     if pixelization == "car":
         Q, dets, resp, gamma, sig = synth.workload(n_det, n_time, seed=59, radius_deg=1.0)
