@@ -288,8 +288,8 @@ class ClockSampler:
 MEASURED_TRAFFIC_PER_SAMPLE = {
     "certified": {"to_map": (834.33e6 + 3.78e6) / 2e8,
                   "from_map": (835.40e6 + 747.14e6) / 2e8},
-    "mixed": {"to_map": (809.487e6 + 9.860e6) / 2e8,
-              "from_map": (809.183e6 + 752.803e6) / 2e8},
+    "mixed": {"to_map": (807.045e6 + 13.405e6) / 2e8,
+              "from_map": (806.769e6 + 790.061e6) / 2e8},
 }
 # Float64-pipe lane operations per sample of the float64 path's to_map
 # (ncu sm__inst_executed_pipe_fp64.sum x 32 / samples, 200 detectors x 1M)
@@ -298,8 +298,8 @@ FP64_OPS_PER_SAMPLE_TO_MAP = 1.018354e9 * 32 / 2e8
 FP64_LANE_OPS_PER_S = 5.0e11
 # The same for the Precomp kernels (ncu, 100 detectors x 1M samples; from_map:
 # k_pc_from_map4, the per-call map split's 0.17 GB left out).
-MEASURED_TRAFFIC_PRECOMP = {"to_map": (2.400758e9 + 3.643e6) / 1e8,
-                            "from_map": (2.401953e9 + 391.81e6) / 1e8}
+MEASURED_TRAFFIC_PRECOMP = {"to_map": (2.400927e9 + 3.107e6) / 1e8,
+                            "from_map": (2.401793e9 + 391.814e6) / 1e8}
 
 
 def algorithmic_bytes(c, op):
