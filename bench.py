@@ -468,6 +468,12 @@ def run_ours(args, c, rank, world, lean=False):
     return res, N
 
 
+# Page-locked host <-> device copy rates of a GB300 machine (torch copies of a
+# 4 GiB buffer, one to eight concurrent streams alike): 209-211 GB/s to the
+# device, 192-193 GB/s back; 171 GB/s each way when both run at once.
+HOST_COPY_GBS = {"h2d": 210.0, "d2h": 193.0}
+
+
 def run_e2e(args, c, eng, q, dets, resp, sig_dev, dev):
     """Same step through the public API with pinned host buffers."""
     import torch
@@ -521,11 +527,19 @@ def run_e2e(args, c, eng, q, dets, resp, sig_dev, dev):
     h2d = nb_sig + nb_map + nb_point + nb_map + nb_point
     d2h = nb_map + nb_sig
     from so3g_gb300 import projeng
+    # The host link bounds this step: to_map's upload has to finish before
+    # from_map can read the map it made, so the two directions run one
+    # after the other at the copy engines' rate.
+    link_ms = (h2d / HOST_COPY_GBS["h2d"] + d2h / HOST_COPY_GBS["d2h"]) / 1e6
     return {"value": N / dt, "unit": "samples/s", "h2d_bytes_per_step": int(h2d),
             "d2h_bytes_per_step": int(d2h), "ms_per_step": dt * 1e3,
             "ms_per_step_median": float(np.median(per_step)) * 1e3,
             "ms_steps": [round(x * 1e3, 2) for x in per_step],
             "estimator": "mean of %d individually timed steps" % steps,
+            "host_link": {"bound": "host<->device copies, one direction after the other",
+                          "copy_gbs": HOST_COPY_GBS, "bound_ms": link_ms,
+                          "frac_median_step": link_ms / (float(np.median(per_step)) * 1e3),
+                          "frac_mean_step": link_ms / (dt * 1e3)},
             "op_ms": {k: float(np.median(v)) for k, v in parts.items()},
             "step": "to_map(host map, page-locked host signal) + from_map(host map, "
                     "signal=None) -> new host signal",
