@@ -274,6 +274,85 @@ def test_cfg2_slice(orc, gpulib, name):
     assert r <= RTOL_MIXED
 
 
+@pytest.mark.parametrize("name", ["certified", "mixed"])
+def test_cfg2_tiled_slice(orc, gpulib, name):
+    """The cfg2 slice on the map cut into 100 x 100 tiles: every sample's
+    pixel through a probe map, to_map per pixel and from_map per sample,
+    against the oracle on the same tiled maps (the tiled pixelizor's
+    truncation at a map's low edges: test_gpu_mixed.py's tiled maps and the
+    fuzz sweep)."""
+    import torch
+    from oracle import pack_tiles, unpack_tiles
+    c, p, q, d, resp = _workload("cfg2", n_det=50, every=20, tiled=True)
+    sig = _signal(len(d), c["n_time"], seed=3)
+    mode = MODES[name]
+    dev = torch.device("cuda", 0)
+    qd, dd, rd = (torch.from_numpy(x).to(dev) for x in (q, d, resp))
+    # Pixels: T-only tiles holding 1 + the parent map's index.
+    engT = p.get_ProjEng("T")
+    engT.pointing = mode
+    nx = engT.naxis[1]
+    ty, tx = engT.tile_shape
+    ntx = engT.tile_grid[1]
+    probe = []
+    for i in range(engT._n_tile()):
+        sh = tuple(engT._tile_pix_shape(i))
+        r, cc = divmod(i, ntx)
+        iy, ix = r * ty + np.arange(sh[0]), cc * tx + np.arange(sh[1])
+        probe.append((1. + iy[:, None] * nx + ix[None, :]).reshape((1,) + sh))
+    ones = np.ones((len(d), 2), np.float32)
+    got = engT.from_map([torch.from_numpy(t).to(dev) for t in probe], qd, dd,
+                        torch.from_numpy(ones).to(dev), None).cpu().numpy()
+    want = np.zeros(got.shape, np.float32)
+    flat, offs = pack_tiles(probe)
+    orc.from_map(_pz(engT, _abi.POINTING_EXACT), q, d, ones, flat, want, tile_offset=offs)
+    n_bad = int(np.count_nonzero(got.view(np.int32) != want.view(np.int32)))
+    print("cfg2 tiled slice %s: pixel mismatches %d of %d" % (name, n_bad, want.size))
+    assert n_bad == 0
+    del got, want, probe
+    # to_map per pixel against the pixel's hit-weighted scale.
+    eng = p.get_ProjEng("TQU")
+    eng.pointing = mode
+    shapes = [(3,) + tuple(eng._tile_pix_shape(i)) for i in range(eng._n_tile())]
+    gt = eng.to_map([torch.zeros(sh, dtype=torch.float64, device=dev) for sh in shapes],
+                    qd, dd, rd, torch.from_numpy(sig).to(dev), None, None)
+    got = np.concatenate([t.cpu().numpy().reshape(3, -1) for t in gt], axis=1)
+    zeros = [np.zeros(sh) for sh in shapes]
+    flat, offs = pack_tiles(zeros)
+    orc.to_map(_pz(eng, _abi.POINTING_EXACT), q, d, resp, sig, None, flat, tile_offset=offs)
+    want_tiles = unpack_tiles(flat, offs, zeros)
+    want = np.concatenate([t.reshape(3, -1) for t in want_tiles], axis=1)
+    amp = np.max(np.abs(resp), axis=1)
+    r_amp = np.stack([amp, amp], axis=1).astype(np.float32)
+    zT = [np.zeros((1,) + sh[1:]) for sh in shapes]
+    flT, ofT = pack_tiles(zT)
+    orc.to_map(_pz(eng, _abi.POINTING_EXACT, 1), q, d, r_amp, np.abs(sig), None, flT,
+               tile_offset=ofT)
+    scale = np.concatenate([t.reshape(-1) for t in unpack_tiles(flT, ofT, zT)])
+    rtol = RTOL_MIXED if name == "mixed" else RTOL_EXACT
+    rel, glob = _check_map(got, want, scale, 3, rtol, "to_map")
+    print("cfg2 tiled slice %s to_map: max error / hit scale %.2e, / max|map| %.2e" %
+          (name, rel, glob))
+    del got, gt
+    # from_map of the oracle's map, per sample.
+    got = eng.from_map([torch.from_numpy(t).to(dev) for t in want_tiles], qd, dd, rd,
+                       None).cpu().numpy()
+    ws = np.zeros(got.shape, np.float32)
+    flat, offs = pack_tiles(want_tiles)
+    orc.from_map(_pz(eng, _abi.POINTING_EXACT), q, d, resp, flat, ws, tile_offset=offs)
+    if name != "mixed":
+        assert int(np.count_nonzero(got.view(np.int32) != ws.view(np.int32))) == 0
+        return
+    mabs = [np.abs(t).sum(axis=0, keepdims=True) for t in want_tiles]
+    fa, oa = pack_tiles(mabs)
+    sc = np.zeros(got.shape, np.float32)
+    orc.from_map(_pz(eng, _abi.POINTING_EXACT, 1), q, d, r_amp, fa, sc, tile_offset=oa)
+    r = float((np.abs(got.astype(np.float64) - ws) /
+               np.maximum(sc.astype(np.float64), 1e-30)).max())
+    print("cfg2 tiled slice %s from_map: max error / sample scale %.2e" % (name, r))
+    assert r <= RTOL_MIXED
+
+
 # -- cfg3: HEALPix nside 1024, 4e7 samples -----------------------------------------
 
 @pytest.mark.parametrize("tiled", [False, True])
