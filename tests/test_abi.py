@@ -55,6 +55,20 @@ def test_library_state_calls_without_gpu(lib):
     assert lib.so3g_launch_count() >= 0
 
 
+def test_chunked_threshold_setter_without_gpu(lib):
+    """so3g_set_chunked_min_samples stores the threshold and returns the
+    previous one (3e7 at load); negative values count as 0."""
+    import so3g_gb300
+    old = so3g_gb300.set_chunked_min_samples(12345)
+    try:
+        assert old >= 0
+        assert so3g_gb300.set_chunked_min_samples(-5) == 12345
+        assert so3g_gb300.set_chunked_min_samples(1 << 40) == 0
+        assert lib.so3g_set_chunked_min_samples(old) == 1 << 40
+    finally:
+        so3g_gb300.set_chunked_min_samples(old)
+
+
 def test_struct_layout_matches_header(tmp_path):
     from so3g_gb300 import _abi
     import ctypes
